@@ -1,0 +1,334 @@
+"""Benchmark of the GB300 spectrometer on the production configuration.
+
+Workload (one "step" = one GPU input buffer of Nb = 2 blocks):
+  64 coarse channels, 2 polarisations, 8-bit complex Gaussian voltages
+  (sigma 20, clipped), Ntpb = 524288 time samples per block (128 MiB blocks,
+  256 MiB per buffer), three simultaneous products Nfft 2^20 / 8 / 1024 with
+  Nint 51 / 128 / 3072, total power (the headline) and full pol (Npolout 4,
+  reported alongside).
+
+Metric: RAW-in GB/s (RAW bytes of the step / step time).
+  value  device-resident throughput: the buffer is in HBM, the timed region
+         is K x rawspec_start_processing (kernels + dumps to pinned host
+         memory), timed with CUDA events on the library's stream;
+  e2e    through the C-ABI from pinned host blocks: K x
+         (rawspec_copy_blocks_to_gpu + rawspec_start_processing +
+         rawspec_wait_for_completion), wall clock.
+
+`--impl reference` times the CPU restatement of the same chain (the
+reference has no CPU implementation of its spectrometer; the OpenMP FP32
+port under oracle/ stands in) with all host threads, on the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NC, NP, NTPB, NBITS = 64, 2, 524288, 8
+PRODUCTS = [(1 << 20, 51), (8, 128), (1024, 3072)]
+SIGMA = 20.0
+BLOCK_BYTES = NC * NTPB * NP * 2
+WORKLOAD = "production shape: 64 ch x 2 pol int8, Ntpb 524288 (128 MiB blocks), Nfft 2^20/8/1024, Nint 51/128/3072"
+
+
+def products(npol):
+    return [(nt, na, npol) for nt, na in PRODUCTS]
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(ctx, i: int, nt: int, na: int, npol: int) -> float:
+    """RAW bytes of the buffer read once plus the product's integrated output
+    bytes amortised per buffer: |P| * Nc * Nt * 4 * Nss / Na."""
+    raw = 2 * BLOCK_BYTES
+    nss = (2 * NTPB) // nt
+    return raw + abs(npol) * NC * nt * 4 * nss / na
+
+
+def load_traffic() -> dict:
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return {}
+    return {}
+
+
+def cpu_sample_run(nthreads: int, nc_sample: int, reps: int = 1) -> tuple[float, float]:
+    """Times the OpenMP FP32 CPU chain on nc_sample channels of one buffer of
+    the workload; returns (GB/s of RAW input, seconds)."""
+    from oracle import oracle as O
+    from rawspec_gb300 import synth
+    blocks = synth.gaussian_blocks(2, nc_sample, NTPB, NP, sigma=SIGMA, seed=1)
+    cfg = O.make_cfg(nc_sample, NP, NTPB, 2, NBITS, products(1))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.run_cpu(cfg, blocks, nthreads=nthreads)
+    dt = (time.perf_counter() - t0) / reps
+    return blocks.nbytes / dt / 1e9, dt
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the chain (kind "port") with all host threads."""
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    threads = O.lib().cpu_max_threads()
+    nc_sample = max(8, threads)
+    for _ in range(args.warmup):
+        cpu_sample_run(threads, nc_sample)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, dt = cpu_sample_run(threads, nc_sample)
+        vals.append(v)
+        secs += dt
+    value = statistics.median(vals)
+    sample = f"{nc_sample} of 64 channels x 1 buffer (2 blocks) per step, all three products, total power"
+    line = {
+        "metric": "RAW-in GB/s", "value": value, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded complex Gaussian int8)",
+        "config": {"workload": WORKLOAD, "npolout": 1, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_native(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    from rawspec_gb300 import api, synth
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    blocks = synth.gaussian_blocks(2, NC, NTPB, NP, sigma=SIGMA, seed=1 + rank)
+    results = {}
+    for npol in (1, 4):
+        spec = api.Spectrometer(NC, NP, NTPB, NBITS, products(npol), gpu_index=local_rank, collect=False)
+        lib = spec.lib
+        cp = C.byref(spec.ctx)
+        stream = torch.cuda.ExternalStream(spec.stream(), device=local_rank)
+        spec.load_blocks(blocks)
+        spec.copy_to_gpu()
+        # device-resident timed region
+        for _ in range(args.warmup):
+            spec.start()
+        spec.wait()
+        spec.reset_profile()
+        spec.set_profiling(True)
+        l0 = spec.kernel_launches()
+        sampler = ClockSampler(local_rank)
+        sampler.start()
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            if lib.rawspec_start_processing(cp, 1) != 0:
+                raise RuntimeError("start_processing failed")
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        clocks = sampler.stop()
+        launches = spec.kernel_launches() - l0
+        ms = max_over_ranks(e0.elapsed_time(e1))
+        spec.wait()
+        prof = {}
+        for k, name in enumerate(api.KERNEL_CLASS_NAMES):
+            t, n = spec.profile(k)
+            prof[name] = (t, n)
+        spec.set_profiling(False)
+        # end-to-end through the C-ABI from pinned host blocks
+        for _ in range(max(1, args.warmup // 2)):
+            spec.copy_to_gpu()
+            spec.start()
+            spec.wait()
+        sizes = [spec.ctx.h_pwrbuf_size[i] for i in range(3)]
+        nis = [spec.product_info(i)[1] for i in range(3)]
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            if lib.rawspec_copy_blocks_to_gpu(cp, 0, 0, 2) != 0:
+                raise RuntimeError("copy failed")
+            if lib.rawspec_start_processing(cp, 1) != 0:
+                raise RuntimeError("start_processing failed")
+            if lib.rawspec_wait_for_completion(cp) != 0:
+                raise RuntimeError("wait failed")
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+        # device->host dump bytes per step (dump schedule over the timed steps)
+        start = args.warmup + max(1, args.warmup // 2) + args.steps
+        d2h = 0
+        for i in range(3):
+            n_dumps = (start + args.steps) // nis[i] - start // nis[i]
+            d2h += n_dumps * sizes[i]
+        results[npol] = dict(ms=ms, prof=prof, launches=launches, clocks=clocks, e2e_s=e2e_s,
+                             d2h=d2h / args.steps, device_bytes=int(lib.rawspec_gb300_device_bytes(cp)))
+        spec.close()
+
+    r = results[1]
+    step_bytes = 2 * BLOCK_BYTES
+    value = world * step_bytes * args.steps / (r["ms"] / 1e3) / 1e9
+    e2e = world * step_bytes * args.steps / r["e2e_s"] / 1e9
+    # dominant kernel class of the headline run
+    prof = r["prof"]
+    kernel_classes = ["small", "finalize", "large_a", "large_b", "ics", "expand4"]
+    dom = max(kernel_classes, key=lambda k: prof[k][0])
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    # algorithmic bytes per launch of the dominant class
+    if dom in ("large_a", "large_b"):
+        alg = algorithmic_bytes(None, 0, PRODUCTS[0][0], PRODUCTS[0][1], 1)
+        dom_name = "k_large_a + k_large_b (Nfft 2^20)"
+        t_ms = prof["large_a"][0] + prof["large_b"][0]
+        n = prof["large_a"][1]
+    else:
+        idx = [1, 2]
+        alg = sum(algorithmic_bytes(None, i, PRODUCTS[i][0], PRODUCTS[i][1], 1) for i in idx) / len(idx)
+        dom_name = f"k_{dom}"
+        t_ms, n = prof[dom]
+    achieved = alg / (t_ms / max(n, 1) / 1e3) / 1e9 if n else None
+    traffic = load_traffic().get(dom_name.split()[0])
+    line = {
+        "metric": "RAW-in GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded complex Gaussian int8, sigma 20)",
+        "config": {"workload": WORKLOAD, "npolout": 1, "step": "one 2-block input buffer (256 MiB RAW)",
+                   "l2": "inputs larger than L2 (256 MiB per step, resident)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": step_bytes,
+                "d2h_bytes_per_step": int(r["d2h"])},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "peak_source": peak_src,
+                     "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()}},
+        "npolout4": {"value": world * step_bytes * args.steps / (results[4]["ms"] / 1e3) / 1e9,
+                     "e2e": world * step_bytes * args.steps / results[4]["e2e_s"] / 1e9,
+                     "ms_per_step": results[4]["ms"] / args.steps},
+        "device_bytes": r["device_bytes"],
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import oracle as O
+        threads = O.lib().cpu_max_threads()
+        nc_sample = max(8, threads)
+        v, dt = cpu_sample_run(threads, nc_sample)
+        line["cpu_baseline"] = {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
+                                "sample": f"{nc_sample} of 64 channels x 1 buffer, all three products, "
+                                          f"total power, {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=24)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["native", "reference"], default="native")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local_rank = rank_info()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import __graft_entry__
+    __graft_entry__.build()
+    return run_native(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,34 @@
+"""Build recipe of the CPU restatements under oracle/ (test infrastructure).
+
+Produces oracle/_build/liboracle.so from rawspec_oracle.c (FP64 checker) and
+rawspec_cpu.c (FP32 OpenMP chain used as the CPU baseline) with gcc.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "liboracle.so"
+SRCS = [HERE / "rawspec_oracle.c", HERE / "rawspec_cpu.c"]
+DEPS = SRCS + [HERE / "rawspec_oracle.h", Path(__file__)]
+
+
+def build(force: bool = False) -> Path:
+    if not force and LIB.exists() and all(p.stat().st_mtime <= LIB.stat().st_mtime for p in DEPS):
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-shared", "-fopenmp", "-o", str(tmp), *map(str, SRCS), "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,184 @@
+// fft_core.cuh -- the FFT engine of the spectrometer kernels.
+//
+// Two levels:
+//   * dft_regs<R>: an R-point DFT (R a power of two <= 32) held entirely in
+//     registers; radix-2 decimation in frequency with compile-time twiddles,
+//     natural order in and out.
+//   * GroupFFT<N, R, NV>: an N-point FFT computed by a group of T = N/R
+//     threads, each holding R values of NV independent vectors (the two
+//     polarisations share every twiddle).  Stockham auto-sort passes of radix
+//     R (a smaller radix for the last pass when N is not a power of R), with
+//     one shared-memory exchange between passes.  On entry thread j holds
+//     x[j + m*T] in v[.][m]; on exit it holds X[j + m*T].  The formulation is
+//     the classic per-thread Stockham iteration (Govindaraju et al., SC08).
+//
+// All FFTs here are forward, exp(-2 pi i k n / N), unnormalised; the inverse
+// transform is obtained by the index reversal X_inv[k] = X_fwd[(N-k) mod N]
+// applied where results are stored.
+#pragma once
+
+#include "common.cuh"
+
+namespace rsg {
+
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
+__host__ __device__ constexpr int bitrev(int x, int bits) {
+  return bits == 0 ? 0 : ((x & 1) << (bits - 1)) | bitrev(x >> 1, bits - 1);
+}
+
+// Compile-time bit-reversal permutation of a register array.
+template <int R, int M>
+struct BitrevSwap {
+  static __device__ __forceinline__ void apply(float2 (&v)[R]) {
+    constexpr int BR = bitrev(M, ilog2(R));
+    if constexpr (M < BR) {
+      const float2 t = v[M];
+      v[M] = v[BR];
+      v[BR] = t;
+    }
+    BitrevSwap<R, M + 1>::apply(v);
+  }
+};
+template <int R>
+struct BitrevSwap<R, R> {
+  static __device__ __forceinline__ void apply(float2 (&)[R]) {}
+};
+
+// In-register DFT of R points (R = 1, 2, 4, 8, 16, 32), natural order.
+template <int R>
+__device__ __forceinline__ void dft_regs(float2 (&v)[R]) {
+  if constexpr (R > 1) {
+#pragma unroll
+    for (int len = R; len >= 2; len >>= 1) {
+      const int half = len >> 1;
+#pragma unroll
+      for (int i = 0; i < R; i += len) {
+#pragma unroll
+        for (int k = 0; k < half; ++k) {
+          const float2 a = v[i + k];
+          const float2 b = v[i + k + half];
+          v[i + k] = cadd(a, b);
+          v[i + k + half] = twiddle_fwd(csub(a, b), k, len);
+        }
+      }
+    }
+    // Outputs are in bit-reversed order: undo with compile-time swaps.
+    BitrevSwap<R, 0>::apply(v);
+  }
+}
+
+// DFT over a strided subset of a register array: elements v[off + s*STRIDE],
+// s = 0..RP-1, with RP*STRIDE <= R.
+template <int RP, int STRIDE, int R>
+__device__ __forceinline__ void dft_subset(float2 (&v)[R], int off) {
+  float2 t[RP];
+#pragma unroll
+  for (int s = 0; s < RP; ++s) t[s] = v[off + s * STRIDE];
+  dft_regs<RP>(t);
+#pragma unroll
+  for (int s = 0; s < RP; ++s) v[off + s * STRIDE] = t[s];
+}
+
+// Shared-memory index with a padding word every 16 complex values, which
+// keeps the strided writes of the Stockham passes free of bank conflicts:
+// element e lives at e + (e >> 4).  GroupFFT computes these positions as a
+// per-thread base plus compile-time offsets, which is exact because every
+// pass's write stride Ns*R and read stride T are powers of two.
+__device__ __forceinline__ int smem_pad(int e) { return e + (e >> 4); }
+__host__ __device__ constexpr int smem_padded_len(int n) { return n + (n >> 4) + 1; }
+
+// Number of radix-R passes and the radix of the trailing pass.
+template <int N, int R>
+struct FftShape {
+  static constexpr int T = N / R;                       // threads per FFT
+  static constexpr int LOGN = ilog2(N);
+  static constexpr int LOGR = ilog2(R);
+  static constexpr int FULL = (LOGR == 0) ? 0 : LOGN / LOGR;     // radix-R passes
+  static constexpr int RLAST = (LOGR == 0) ? 1 : (1 << (LOGN - FULL * LOGR));
+  static constexpr int PASSES = FULL + (RLAST > 1 ? 1 : 0);
+};
+
+// Group FFT.  tw: table of W_N^m = exp(-2 pi i m / N), m in [0, N), in shared
+// (or global) memory.  sm: this group's exchange buffers, NV buffers of
+// smem_padded_len(N) float2 each, spaced by `sm_stride` float2.  SYNC is a
+// functor performing the barrier required between the group's threads.
+template <int N, int R, int NV>
+struct GroupFFT {
+  using S = FftShape<N, R>;
+  static constexpr int T = S::T;
+
+  template <typename Sync>
+  static __device__ __forceinline__ void run(float2 (&v)[NV][R], int j, float2* sm, int sm_stride,
+                                             const float2* __restrict__ tw, Sync sync) {
+    if constexpr (T == 1) {
+      // One thread holds the whole transform.
+#pragma unroll
+      for (int q = 0; q < NV; ++q) dft_regs<R>(v[q]);
+    } else {
+      int Ns = 1;
+#pragma unroll
+      for (int p = 0; p < S::FULL; ++p) {
+        // Twiddles (identity on the first pass).
+        if (p > 0) {
+          const int k = j & (Ns - 1);
+          const int step = N / (Ns * R);  // tw index of element r is k*r*step
+#pragma unroll
+          for (int r = 1; r < R; ++r) {
+            const float2 w = tw[k * r * step];
+#pragma unroll
+            for (int q = 0; q < NV; ++q) v[q][r] = cmul(v[q][r], w);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < NV; ++q) dft_regs<R>(v[q]);
+        const bool last = (p == S::FULL - 1) && (S::RLAST == 1);
+        if (!last) {
+          // Padded write positions idxD + r*Ns as a runtime base plus a
+          // compile-time offset per r (see smem_pad).
+          const int lo = j & (Ns - 1);
+          const int hi = j / Ns;
+          const int idxD = hi * Ns * R + lo;
+          const int wbase = idxD + ((hi * Ns * R) >> 4) + (Ns >= 16 ? (lo >> 4) : 0);
+#pragma unroll
+          for (int q = 0; q < NV; ++q)
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              const int off = Ns >= 16 ? r * (Ns + (Ns >> 4)) : r * Ns + ((r * Ns) >> 4);
+              sm[q * sm_stride + wbase + off] = v[q][r];
+            }
+          sync();
+          const int rbase = j + (T >= 16 ? (j >> 4) : 0);
+#pragma unroll
+          for (int q = 0; q < NV; ++q)
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+              const int off = T >= 16 ? m * (T + (T >> 4)) : m * T + ((m * T) >> 4);
+              v[q][m] = sm[q * sm_stride + rbase + off];
+            }
+          sync();
+        }
+        Ns *= R;
+      }
+      if constexpr (S::RLAST > 1) {
+        // Trailing pass of radix RL < R: thread j computes Q = R/RL
+        // butterflies b = j + q*T on elements m = q + r*Q.
+        constexpr int RL = S::RLAST;
+        constexpr int Q = R / RL;
+#pragma unroll
+        for (int qb = 0; qb < Q; ++qb) {
+          const int b = j + qb * T;  // k = b (b < Ns); tw index b*r
+#pragma unroll
+          for (int r = 1; r < RL; ++r) {
+            const float2 w = tw[b * r];
+#pragma unroll
+            for (int q = 0; q < NV; ++q) v[q][qb + r * Q] = cmul(v[q][qb + r * Q], w);
+          }
+#pragma unroll
+          for (int q = 0; q < NV; ++q) dft_subset<RL, Q>(v[q], qb);
+        }
+      }
+    }
+  }
+};
+
+}  // namespace rsg

@@ -1,0 +1,126 @@
+// internal.h -- launch descriptors shared by the host API (rawspec_api.cu)
+// and the kernel translation units.  Plain C++ types only.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rsg {
+
+// Output polarisation modes (the reference's Npolout values, with total
+// power split by the number of input polarisations).
+enum PolMode : int { POL_TP = 0, POL_FULL = 4, POL_STOKES = -4 };
+
+// Accumulation mode of a kernel's output.
+enum AccMode : int { ACC_WRITE = 0, ACC_ADD = 1 };
+
+// Sample formats of the device input buffer (int4 input is expanded to int8
+// before processing).
+enum SampleFormat : int { FMT_I8 = 0, FMT_I16 = 1 };
+
+// ---------------------------------------------------------------------------
+// Fused small-FFT product kernel (N <= 4096): unpack, FFT, detect, integrate.
+// An "integration unit" is a run of M consecutive spectra of one channel that
+// ends in one output spectrum (M = Na when an integration completes within
+// the buffer, M = spectra per buffer otherwise).
+// ---------------------------------------------------------------------------
+struct SmallLaunch {
+  // selection
+  int logN = 0;      // log2 of the FFT length
+  int fmt = 0;       // SampleFormat
+  int nv = 2;        // input polarisations
+  int pol = POL_TP;  // PolMode
+  // geometry (filled by small_configure)
+  int tpb = 0, sets = 1, chunks = 1, spc = 0, grid = 0;
+  size_t smem = 0;
+  // problem
+  int Nc = 0, M = 0, units_per_chan = 0, n_units = 0;
+  long long chan_stride = 0;  // samples per channel in the device buffer
+  // buffers
+  const void* in = nullptr;
+  float* out = nullptr;       // [units_per_chan][|P|][Nc][N], FFT-shifted
+  float* partial = nullptr;   // [n_units][chunks][|P|][N] (chunks > 1)
+  const float2* tw = nullptr; // W_N^m, m < N
+  // per call
+  int mode = ACC_WRITE, inverse = 0, conj = 0;
+};
+
+// Chooses block size, units per block and chunks per unit.  target_ctas is
+// the number of CTAs that fills the GPU.  Returns 0, or -1 if N is out of
+// range.  partial_floats receives the scratch the launch needs (0 if none).
+int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats);
+cudaError_t small_launch(const SmallLaunch& L, cudaStream_t s);
+// Raises the kernel's dynamic shared-memory limit on the current device.
+cudaError_t small_prepare(const SmallLaunch& L);
+
+// Sums the per-chunk partial spectra of every unit in chunk order and writes
+// (or adds) them FFT-shifted into the output.
+struct FinalizeLaunch {
+  const float* partial = nullptr;
+  float* out = nullptr;
+  int n_units = 0, chunks = 0, np = 1, N = 0, Nc = 0, units_per_chan = 0;
+  int mode = ACC_WRITE, inverse = 0;
+};
+cudaError_t finalize_launch(const FinalizeLaunch& L, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Four-step large FFT (4096 < N <= 2^22): N = N1 * N2.
+//   pass A: N2-point FFTs down the columns n1 of x[n1 + N1*n2], twiddled by
+//           W_N^(n1*k2), written to scratch as [slab][pol][k2][n1];
+//   pass B: N1-point FFTs along the rows k2, detection, integration.
+// A slab is one (channel, spectrum) pair.
+// ---------------------------------------------------------------------------
+struct LargeLaunch {
+  int logN = 0, logN1 = 0, logN2 = 0;
+  int fmt = 0, nv = 2, pol = POL_TP;
+  int Nc = 0, Nss = 0;            // channels, spectra per channel in a buffer
+  int M = 0, units_per_chan = 0, n_units = 0, chunks = 1, spc = 0;
+  long long chan_stride = 0;
+  const void* in = nullptr;
+  float2* scratch = nullptr;      // [Nc*Nss][nv][N2][N1]
+  float* out = nullptr;
+  float* partial = nullptr;
+  const float2* twN2 = nullptr;   // W_N2^m
+  const float2* twN1 = nullptr;   // W_N1^m
+  const float2* twLo = nullptr;   // W_N^i, i < 2^h
+  const float2* twHi = nullptr;   // W_N^(i*2^h), i < N / 2^h
+  int h = 0;
+  int mode = ACC_WRITE, inverse = 0, conj = 0;
+};
+int large_configure(LargeLaunch& L, int target_ctas, size_t* scratch_float2, size_t* partial_floats);
+cudaError_t large_launch_a(const LargeLaunch& L, cudaStream_t s);
+cudaError_t large_launch_b(const LargeLaunch& L, cudaStream_t s);
+// Raises both kernels' dynamic shared-memory limits on the current device.
+cudaError_t large_prepare(const LargeLaunch& L);
+
+// ---------------------------------------------------------------------------
+// Auxiliary kernels.
+// ---------------------------------------------------------------------------
+// W_n^m = exp(-2 pi i m stride / n) for m < count, computed in FP64 with
+// sincospi and rounded to float.
+cudaError_t twiddle_fill(float2* dst, long long count, long long n, long long stride, cudaStream_t s);
+
+// 4-bit complex expansion: for each of num_blocks blocks and each channel,
+// bytes of the packed staging buffer become (re, im) int8 pairs in the input
+// buffer (high nibble real, low nibble imaginary, sign-extended).
+struct Expand4Launch {
+  const uint8_t* packed = nullptr;  // [Nc][Nb*blk_bytes_packed]
+  int8_t* out = nullptr;            // [Nc][Nb*blk_bytes_packed*2]
+  int Nc = 0, Nb = 0;
+  long long blk_bytes_packed = 0;   // Ntpb * Np
+  int dst_block = 0, num_blocks = 0;
+};
+cudaError_t expand4_launch(const Expand4Launch& L, cudaStream_t s);
+
+// Weighted incoherent sum over antennas of FFT-shifted spectra:
+// ics[d][p][c][f] = sum_a w[a] * pwr[d][p][a*Nca + c][f] (sequential in a).
+struct IcsLaunch {
+  const float* pwr = nullptr;
+  float* ics = nullptr;
+  const float* w = nullptr;
+  int Nd = 0, np = 1, Nc = 0, Nant = 1, N = 0;
+};
+cudaError_t ics_launch(const IcsLaunch& L, cudaStream_t s);
+
+}  // namespace rsg

@@ -1,0 +1,113 @@
+// k_aux.cu -- plan-time twiddle tables, 4-bit expansion and the weighted
+// incoherent sum across antennas.
+#include <algorithm>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace rsg {
+
+// W_n^(m*stride) = exp(-2 pi i m stride / n), FP64 sincospi rounded to float.
+// Used only when a context is initialised.
+__global__ void k_twiddle(float2* dst, long long count, long long n, long long stride) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < count;
+       m += (long long)gridDim.x * blockDim.x) {
+    const long long e = (m * stride) % n;
+    double s, c;
+    sincospi(2.0 * (double)e / (double)n, &s, &c);
+    dst[m] = make_float2((float)c, (float)(-s));
+  }
+}
+
+cudaError_t twiddle_fill(float2* dst, long long count, long long n, long long stride, cudaStream_t s) {
+  const int blocks = (int)std::min<long long>((count + 255) / 256, 4096);
+  k_twiddle<<<std::max(blocks, 1), 256, 0, s>>>(dst, count, n, stride);
+  return cudaGetLastError();
+}
+
+// 4-bit complex expansion (bit-exact replacement of the reference's LUT
+// kernels complex4_expansion / copy_expand_complex4, rawspec_gpu.cu:342-374):
+// packed byte b -> real = sign-extended high nibble, imag = sign-extended low
+// nibble.  The packed staging buffer already has the reference's corner-turned
+// layout [channel][block][time][pol], so the expansion is a pure stream.
+__device__ __forceinline__ uint32_t expand2(uint32_t b0, uint32_t b1) {
+  // two packed bytes -> four int8 components (re0, im0, re1, im1)
+  const uint32_t r0 = (uint32_t)(uint8_t)((int8_t)(b0 & 0xf0) >> 4);
+  const uint32_t i0 = (uint32_t)(uint8_t)((int8_t)(b0 << 4) >> 4);
+  const uint32_t r1 = (uint32_t)(uint8_t)((int8_t)(b1 & 0xf0) >> 4);
+  const uint32_t i1 = (uint32_t)(uint8_t)((int8_t)(b1 << 4) >> 4);
+  return r0 | (i0 << 8) | (r1 << 16) | (i1 << 24);
+}
+
+__global__ void k_expand4_words(Expand4Launch a) {
+  // one thread per 4 packed bytes; blk_bytes_packed % 4 == 0
+  const long long words_per_seg = a.blk_bytes_packed / 4;
+  const long long total = words_per_seg * a.Nc * a.num_blocks;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long w = i % words_per_seg;
+    const long long seg = i / words_per_seg;
+    const int c = (int)(seg % a.Nc);
+    const int bi = (int)(seg / a.Nc);
+    const int blk = (a.dst_block + bi) % a.Nb;
+    const long long pin = (long long)c * a.Nb * a.blk_bytes_packed + (long long)blk * a.blk_bytes_packed;
+    const uint32_t p = *reinterpret_cast<const uint32_t*>(a.packed + pin + 4 * w);
+    uint2 o;
+    o.x = expand2(p & 0xff, (p >> 8) & 0xff);
+    o.y = expand2((p >> 16) & 0xff, p >> 24);
+    *reinterpret_cast<uint2*>(a.out + 2 * pin + 8 * w) = o;
+  }
+}
+
+__global__ void k_expand4_bytes(Expand4Launch a) {
+  const long long total = a.blk_bytes_packed * a.Nc * a.num_blocks;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long b = i % a.blk_bytes_packed;
+    const long long seg = i / a.blk_bytes_packed;
+    const int c = (int)(seg % a.Nc);
+    const int bi = (int)(seg / a.Nc);
+    const int blk = (a.dst_block + bi) % a.Nb;
+    const long long pin = (long long)c * a.Nb * a.blk_bytes_packed + (long long)blk * a.blk_bytes_packed + b;
+    const uint8_t v = a.packed[pin];
+    a.out[2 * pin] = (int8_t)(v & 0xf0) >> 4;
+    a.out[2 * pin + 1] = (int8_t)(uint8_t)(v << 4) >> 4;
+  }
+}
+
+cudaError_t expand4_launch(const Expand4Launch& L, cudaStream_t s) {
+  const bool words = (L.blk_bytes_packed % 4) == 0;
+  const long long items = (words ? L.blk_bytes_packed / 4 : L.blk_bytes_packed) * L.Nc * L.num_blocks;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((items + 255) / 256, 152LL * 32));
+  if (words) k_expand4_words<<<blocks, 256, 0, s>>>(L);
+  else k_expand4_bytes<<<blocks, 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+// Weighted incoherent sum over antennas (the reference's incoherent_sum,
+// rawspec_gpu.cu:321-340): ics = sum_a w[a] * P[antenna a], accumulated in
+// antenna order with fused multiply-adds from zero.  Both buffers are already
+// FFT-shifted, so the fine-channel index maps straight through.
+__global__ void k_ics(IcsLaunch a) {
+  const int Nca = a.Nc / a.Nant;
+  const long long per_plane = (long long)Nca * a.N;
+  const long long total = (long long)a.Nd * a.np * per_plane;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long within = i % per_plane;   // c*N + f
+    const long long dp = i / per_plane;       // d*np + p
+    const float* src = a.pwr + dp * (long long)a.Nc * a.N + within;
+    float s = 0.0f;
+    for (int ant = 0; ant < a.Nant; ++ant) s = __fmaf_rn(a.w[ant], src[(long long)ant * per_plane], s);
+    a.ics[i] = s;
+  }
+}
+
+cudaError_t ics_launch(const IcsLaunch& L, cudaStream_t s) {
+  const long long total = (long long)L.Nd * L.np * (L.Nc / L.Nant) * L.N;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 152LL * 16));
+  k_ics<<<blocks, 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+}  // namespace rsg

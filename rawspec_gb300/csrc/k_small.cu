@@ -1,0 +1,306 @@
+// k_small.cu -- fused spectrometer kernel for FFT lengths N <= 4096.
+//
+// One launch per output product and input buffer replaces the reference's
+// per-(product, batch, pol) cufftExecC2C calls with their texture load
+// callback and read-modify-write store callbacks (rawspec_gpu.cu:1555-1569,
+// :133-267), the sub-integration `accumulate` kernel (:297-318, :1588-1601)
+// and the FFT-shifting device-to-host copies (:1647-1697):
+//
+//   int8/int16 load + SNORM conversion -> Stockham FFT in registers/shared
+//   memory (both polarisations together) -> detection -> accumulation of the
+//   unit's spectra in registers -> reduction across the CTA's thread groups
+//   -> FFT-shifted store into the dump buffer [Nd][|P|][Nc][N] (or partial
+//   sums when one unit is spread over several CTAs).
+//
+// Nothing but the raw voltages is read and nothing but integrated spectra is
+// written.
+#include <algorithm>
+
+#include "detect.cuh"
+#include "fft_core.cuh"
+#include "internal.h"
+
+namespace rsg {
+
+// R (values per thread per polarisation) is 8: data, twiddles and the 4*R
+// accumulators of the four-plane modes then fit the register cap of two
+// resident CTAs per SM without spilling.
+template <int N, int NP>
+struct SmallCfg {
+  static constexpr int RMAX = 8;
+  static constexpr int R = N < RMAX ? N : RMAX;
+  static constexpr int T = N / R;            // threads per FFT
+  static constexpr int TPB = T > 256 ? T : 256;
+  static constexpr int G = TPB / T;          // FFT groups per CTA
+  static constexpr int MINB = 65536 / (TPB * 128) > 0 ? 65536 / (TPB * 128) : 1;
+};
+
+struct WarpSync {
+  __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+struct BlockSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
+template <int N, int NV, int NP>
+__host__ __device__ constexpr size_t small_smem_bytes() {
+  using C = SmallCfg<N, NP>;
+  const size_t tw = (C::T > 1) ? (size_t)N * sizeof(float2) : 0;
+  const size_t xch = (C::T > 1) ? (size_t)C::G * NV * smem_padded_len(N) * sizeof(float2) : 0;
+  const size_t red = (size_t)C::TPB * C::R * NP * sizeof(float);
+  return tw + (xch > red ? xch : red);
+}
+
+template <int N, int FMT, int NV, int POL>
+__global__ void __launch_bounds__(SmallCfg<N, PolOut<POL>::NP>::TPB, SmallCfg<N, PolOut<POL>::NP>::MINB)
+k_small(SmallLaunch a) {
+  constexpr int NP = PolOut<POL>::NP;
+  using C = SmallCfg<N, NP>;
+  constexpr int R = C::R, T = C::T, G = C::G, TPB = C::TPB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+
+  float2* tw_s = reinterpret_cast<float2*>(smem_raw);
+  float2* xch = tw_s + ((T > 1) ? N : 0);
+  float* red = reinterpret_cast<float*>(xch);
+
+  const int tid = threadIdx.x;
+  const int g = tid / T;   // group within the CTA
+  const int j = tid % T;   // thread within the group
+
+  if constexpr (T > 1) {
+    for (int i = tid; i < N; i += TPB) tw_s[i] = a.tw[i];
+    __syncthreads();
+  }
+
+  // Which unit / spectra this group works on.  The CTA covers `sets` units
+  // (gps groups each) and one chunk of spc spectra of each of them.
+  const int gps = G / a.sets;           // groups per set
+  const int set = g / gps;
+  const int gi = g % gps;
+  const int ublock = blockIdx.x / a.chunks;
+  const int chunk = blockIdx.x % a.chunks;
+  const int unit = ublock * a.sets + set;
+  const int s_begin = chunk * a.spc;
+  const int s_end = min(a.M, s_begin + a.spc);
+  const bool unit_ok = unit < a.n_units;
+  const int c = unit_ok ? unit / a.units_per_chan : 0;
+  const int d = unit_ok ? unit % a.units_per_chan : 0;
+  const long long chan_base = (long long)c * a.chan_stride;
+  const long long unit_first_spec = (long long)d * a.M;
+  const int iters = (a.spc + gps - 1) / gps;
+  const float im_sign = a.conj ? -1.0f : 1.0f;
+
+  float acc[R][NP];
+#pragma unroll
+  for (int m = 0; m < R; ++m)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[m][p] = 0.0f;
+
+  float2* my_xch = xch + (size_t)g * NV * smem_padded_len(N);
+
+  for (int it = 0; it < iters; ++it) {
+    const int s_local = s_begin + gi + it * gps;
+    const bool valid = unit_ok && s_local < s_end;
+    float2 v[NV][R];
+    if (valid) {
+      using W = typename SampleWord<FMT, NV>::type;
+      const W* src = reinterpret_cast<const W*>(a.in) + chan_base + (unit_first_spec + s_local) * N + j;
+      W w[R];
+#pragma unroll
+      for (int m = 0; m < R; ++m) w[m] = __ldg(src + m * T);
+#pragma unroll
+      for (int m = 0; m < R; ++m) {
+        float2 smp[NV];
+        unpack_word(w[m], smp);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q][m] = smp[q];
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < R; ++m)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q][m] = make_float2(0.f, 0.f);
+    }
+    if constexpr (T > 32) {
+      GroupFFT<N, R, NV>::run(v, j, my_xch, smem_padded_len(N), tw_s, BlockSync{});
+    } else {
+      GroupFFT<N, R, NV>::run(v, j, my_xch, smem_padded_len(N), tw_s, WarpSync{});
+    }
+    if (valid) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) {
+        float2 x[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = v[q][m];
+        detect_acc<POL, NV>(acc[m], x, im_sign);
+      }
+    }
+  }
+
+  // Reduce across the groups of each set: red[g][p][m][j].
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < NP; ++p)
+#pragma unroll
+    for (int m = 0; m < R; ++m) red[((g * NP + p) * R + m) * T + j] = acc[m][p];
+  __syncthreads();
+
+  const int set_threads = gps * T;
+  const int t_in_set = tid - set * set_threads;
+  if (!unit_ok) return;
+  for (int o = t_in_set; o < NP * N; o += set_threads) {
+    const int p = o / N;
+    const int k = o - p * N;
+    const int m = k / T;
+    const int jj = k - m * T;
+    float s = 0.0f;
+    for (int q = 0; q < gps; ++q) s += red[(((set * gps + q) * NP + p) * R + m) * T + jj];
+    if (a.chunks > 1) {
+      a.partial[(((size_t)unit * a.chunks + chunk) * NP + p) * N + k] = s;
+    } else {
+      float* dst = a.out + (((size_t)d * NP + p) * a.Nc + c) * N + out_pos(k, N, a.inverse);
+      if (a.mode == ACC_ADD) *dst += s; else *dst = s;
+    }
+  }
+}
+
+// Finalisation of chunked units: fixed-order sum of the chunks' partials.
+__global__ void k_finalize(FinalizeLaunch a) {
+  const long long total = (long long)a.n_units * a.np * a.N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(i % a.N);
+    const long long up = i / a.N;
+    const int p = (int)(up % a.np);
+    const int unit = (int)(up / a.np);
+    const float* src = a.partial + ((size_t)unit * a.chunks * a.np + p) * a.N + k;
+    float s = 0.0f;
+    for (int q = 0; q < a.chunks; ++q) s += src[(size_t)q * a.np * a.N];
+    const int c = unit / a.units_per_chan;
+    const int d = unit % a.units_per_chan;
+    float* dst = a.out + (((size_t)d * a.np + p) * a.Nc + c) * a.N + out_pos(k, a.N, a.inverse);
+    if (a.mode == ACC_ADD) *dst += s; else *dst = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side: configuration and dispatch.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct SmallInfo {
+  int R, T, TPB, G;
+  size_t smem;
+};
+
+template <int N, int NP>
+SmallInfo small_info_np(int nv) {
+  using C = SmallCfg<N, NP>;
+  SmallInfo s{C::R, C::T, C::TPB, C::G, 0};
+  s.smem = nv == 1 ? small_smem_bytes<N, 1, NP>() : small_smem_bytes<N, 2, NP>();
+  return s;
+}
+template <int N>
+SmallInfo small_info(int nv, int pol) {
+  return pol == POL_TP ? small_info_np<N, 1>(nv) : small_info_np<N, 4>(nv);
+}
+
+SmallInfo small_info_dyn(int logN, int nv, int pol) {
+  switch (logN) {
+    case 0: return small_info<1>(nv, pol);
+    case 1: return small_info<2>(nv, pol);
+    case 2: return small_info<4>(nv, pol);
+    case 3: return small_info<8>(nv, pol);
+    case 4: return small_info<16>(nv, pol);
+    case 5: return small_info<32>(nv, pol);
+    case 6: return small_info<64>(nv, pol);
+    case 7: return small_info<128>(nv, pol);
+    case 8: return small_info<256>(nv, pol);
+    case 9: return small_info<512>(nv, pol);
+    case 10: return small_info<1024>(nv, pol);
+    case 11: return small_info<2048>(nv, pol);
+    default: return small_info<4096>(nv, pol);
+  }
+}
+
+template <int N, int FMT, int NV, int POL>
+cudaError_t launch_t(const SmallLaunch& L, cudaStream_t s, bool prep) {
+  auto k = k_small<N, FMT, NV, POL>;
+  if (prep) {  // preparation call: allow the dynamic shared memory
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+  }
+  k<<<L.grid, SmallCfg<N, PolOut<POL>::NP>::TPB, L.smem, s>>>(L);
+  return cudaGetLastError();
+}
+
+template <int N, int FMT>
+cudaError_t launch_pol(const SmallLaunch& L, cudaStream_t s, bool prep) {
+  if (L.nv == 1) return launch_t<N, FMT, 1, POL_TP>(L, s, prep);
+  switch (L.pol) {
+    case POL_FULL: return launch_t<N, FMT, 2, POL_FULL>(L, s, prep);
+    case POL_STOKES: return launch_t<N, FMT, 2, POL_STOKES>(L, s, prep);
+    default: return launch_t<N, FMT, 2, POL_TP>(L, s, prep);
+  }
+}
+
+template <int N>
+cudaError_t launch_fmt(const SmallLaunch& L, cudaStream_t s, bool prep) {
+  return L.fmt == FMT_I16 ? launch_pol<N, FMT_I16>(L, s, prep) : launch_pol<N, FMT_I8>(L, s, prep);
+}
+
+}  // namespace
+
+int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats) {
+  if (L.logN < 0 || L.logN > 12 || L.M < 1 || L.n_units < 1) return -1;
+  const SmallInfo si = small_info_dyn(L.logN, L.nv, L.pol);
+  L.tpb = si.TPB;
+  L.smem = si.smem;
+  const int G = si.G;
+  const int np = L.pol == POL_TP ? 1 : 4;
+  auto pow2_floor = [](int x) { int p = 1; while (p * 2 <= x) p *= 2; return p; };
+  // Groups per unit: at most one per spectrum, and few enough that every
+  // thread of a set has an output to reduce (gps <= |P| * R).
+  int gps = std::min(G, std::min(pow2_floor(np * si.R), pow2_floor(L.M)));
+  L.sets = G / gps;
+  const int ublocks = (L.n_units + L.sets - 1) / L.sets;
+  const int max_chunks = (L.M + gps - 1) / gps;
+  int chunks = (target_ctas + ublocks - 1) / ublocks;
+  chunks = std::max(1, std::min(chunks, max_chunks));
+  L.spc = (L.M + chunks - 1) / chunks;
+  L.chunks = (L.M + L.spc - 1) / L.spc;
+  L.grid = ublocks * L.chunks;
+  *partial_floats = L.chunks > 1 ? (size_t)L.n_units * L.chunks * np * ((size_t)1 << L.logN) : 0;
+  return 0;
+}
+
+static cudaError_t small_dispatch(const SmallLaunch& L, cudaStream_t s, bool prep) {
+  switch (L.logN) {
+    case 0: return launch_fmt<1>(L, s, prep);
+    case 1: return launch_fmt<2>(L, s, prep);
+    case 2: return launch_fmt<4>(L, s, prep);
+    case 3: return launch_fmt<8>(L, s, prep);
+    case 4: return launch_fmt<16>(L, s, prep);
+    case 5: return launch_fmt<32>(L, s, prep);
+    case 6: return launch_fmt<64>(L, s, prep);
+    case 7: return launch_fmt<128>(L, s, prep);
+    case 8: return launch_fmt<256>(L, s, prep);
+    case 9: return launch_fmt<512>(L, s, prep);
+    case 10: return launch_fmt<1024>(L, s, prep);
+    case 11: return launch_fmt<2048>(L, s, prep);
+    case 12: return launch_fmt<4096>(L, s, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t small_prepare(const SmallLaunch& L) { return small_dispatch(L, nullptr, true); }
+cudaError_t small_launch(const SmallLaunch& L, cudaStream_t s) { return small_dispatch(L, s, false); }
+
+cudaError_t finalize_launch(const FinalizeLaunch& L, cudaStream_t s) {
+  const long long total = (long long)L.n_units * L.np * L.N;
+  int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+  if (blocks < 1) blocks = 1;
+  k_finalize<<<blocks, 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+}  // namespace rsg

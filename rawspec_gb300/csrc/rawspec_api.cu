@@ -1,0 +1,874 @@
+// rawspec_api.cu -- the C-ABI of the GB300-native librawspec.
+//
+// Implements the twelve entry points of rawspec.h (reference:
+// rawspec_gpu.cu:404-1836) plus the extensions of rawspec_gb300.h.  The
+// validation and normalisation rules of rawspec_initialize() follow the
+// reference (rawspec_gpu.cu:471-641, 732-782) so that clients observe the same
+// accepted configurations, coercions and error returns; the device-side
+// design is this project's own:
+//
+//  * the device input buffer keeps the reference's corner-turned layout
+//    [channel][Nb*Ntpb][pol][re,im] (one cudaMemcpy2DAsync per block);
+//  * every product keeps one device accumulator laid out exactly like its
+//    host dump buffer h_pwrbuf ([Nd][|P|][Nc][Nt], FFT-shifted), written by
+//    the first buffer of an integration and added to by later ones, so a dump
+//    is a single contiguous device->host copy and no clearing pass is needed;
+//  * no channel batching: all Nc channels are processed by each launch, which
+//    removes the batch cache kernels and their hazards;
+//  * PRE_DUMP is queued before any write to h_pwrbuf/h_icsbuf of a dump and
+//    POST_DUMP after both, on the processing stream (cudaLaunchHostFunc).
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+#include "rawspec.h"
+#include "rawspec_gb300.h"
+
+#define RSG_STR1(s) #s
+#define RSG_STR(s) RSG_STR1(s)
+#ifndef RAWSPEC_GB300_VERSION
+#define RAWSPEC_GB300_VERSION 0.1.0
+#endif
+
+namespace {
+
+using namespace rsg;
+
+constexpr int kMaxLogN = 24;
+
+#define RSG_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t rsg_e_ = (call);                                                         \
+    if (rsg_e_ != cudaSuccess) {                                                         \
+      fprintf(stderr, "got error %s at %s:%d\n", cudaGetErrorName(rsg_e_), __FILE__,     \
+              __LINE__);                                                                 \
+      fflush(stderr);                                                                    \
+      return 1;                                                                          \
+    }                                                                                    \
+  } while (0)
+
+struct Product {
+  int N = 0, logN = 0, np = 1;
+  unsigned Nss = 0, Nd = 0, Nis = 0, Na = 0;
+  bool large = false;
+  float* d_out = nullptr;
+  size_t out_bytes = 0;
+  float* d_ics = nullptr;
+  size_t ics_bytes = 0;
+  float2* d_tw = nullptr;  // small: W_N; large: W_N2 | W_N1 | lo | hi
+  SmallLaunch sl;
+  LargeLaunch ll;
+  int chunks = 1;
+};
+
+struct DumpCb {
+  rawspec_context* ctx;
+  int product;
+};
+
+struct EventPair {
+  int cls;
+  cudaEvent_t a, b;
+};
+
+struct GpuCtx {
+  int device = 0;
+  int sm_count = 152;
+  cudaStream_t stream = nullptr;
+  void* d_in = nullptr;
+  size_t in_bytes = 0;
+  uint8_t* d_in4 = nullptr;
+  size_t in4_bytes = 0;
+  int fmt = FMT_I8;
+  float* d_aws = nullptr;
+  float* d_partial = nullptr;
+  size_t partial_floats = 0;
+  float2* d_scratch = nullptr;
+  size_t scratch_f2 = 0;
+  Product prod[MAX_OUTPUTS];
+  unsigned inbuf_count = 0;
+  bool caller_managed = false;
+  unsigned registered = 0;  // caller blocks page-locked so far
+  DumpCb cb[MAX_OUTPUTS];
+  size_t device_bytes = 0;
+  unsigned long long launches = 0;
+  // profiling
+  bool profiling = false;
+  std::vector<EventPair> pending;
+  std::vector<cudaEvent_t> free_events;
+  double prof_ms[RAWSPEC_GB300_K_COUNT] = {0};
+  unsigned long long prof_n[RAWSPEC_GB300_K_COUNT] = {0};
+};
+
+GpuCtx* G(rawspec_context* ctx) { return reinterpret_cast<GpuCtx*>(ctx->gpu_ctx); }
+
+// ----------------------------------------------------------------------------
+// Profiling helpers.
+// ----------------------------------------------------------------------------
+cudaEvent_t take_event(GpuCtx* g) {
+  if (!g->free_events.empty()) {
+    cudaEvent_t e = g->free_events.back();
+    g->free_events.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+struct ProfScope {
+  GpuCtx* g;
+  int cls;
+  cudaEvent_t a = nullptr;
+  ProfScope(GpuCtx* g_, int cls_) : g(g_), cls(cls_) {
+    if (g->profiling) {
+      a = take_event(g);
+      if (a) cudaEventRecord(a, g->stream);
+    }
+  }
+  ~ProfScope() {
+    if (g->profiling && a) {
+      cudaEvent_t b = take_event(g);
+      if (b) {
+        cudaEventRecord(b, g->stream);
+        g->pending.push_back({cls, a, b});
+      } else {
+        g->free_events.push_back(a);
+      }
+    }
+  }
+};
+
+void collect_profile(GpuCtx* g) {
+  for (auto& p : g->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      g->prof_ms[p.cls] += ms;
+      g->prof_n[p.cls] += 1;
+    }
+    g->free_events.push_back(p.a);
+    g->free_events.push_back(p.b);
+  }
+  g->pending.clear();
+}
+
+// ----------------------------------------------------------------------------
+// Validation (reference rules, rawspec_gpu.cu:471-641 and :732-760).
+// ----------------------------------------------------------------------------
+bool is_pow2(unsigned x) { return x && !(x & (x - 1)); }
+int ilog2u(unsigned x) { int l = 0; while ((1u << l) < x) ++l; return l; }
+
+int validate_impl(rawspec_context* ctx, bool* expanded) {
+  if (ctx->No == 0 || ctx->No > MAX_OUTPUTS) {
+    fprintf(stderr, "output products must be in range [1..%d], not %d\n", MAX_OUTPUTS, ctx->No);
+    fflush(stderr);
+    return 1;
+  }
+  if (ctx->Np == 0 || ctx->Np > 2) {
+    fprintf(stderr, "number of polarizations must be in range [1..2], not %d\n", ctx->Np);
+    fflush(stderr);
+    return 1;
+  }
+  for (unsigned i = 0; i < ctx->No; i++) {
+    if (abs(ctx->Npolout[i]) != 4 || ctx->Np != 2) ctx->Npolout[i] = 1;
+  }
+  if (ctx->Ntpb == 0) {
+    fprintf(stderr, "number of time samples per block cannot be zero\n");
+    fflush(stderr);
+    return 1;
+  }
+  if (ctx->Nbps == 0) ctx->Nbps = 8;
+  if (ctx->Nbps != 4 && ctx->Nbps != 8 && ctx->Nbps != 16) {
+    fprintf(stderr, "Number of bits per sample in raw header must be 4, 0/8, or 16\n");
+    fprintf(stderr, "Observed a value of %d\n", ctx->Nbps);
+    fflush(stderr);
+    return 1;
+  }
+  *expanded = ctx->Nbps == 4;
+  if (ctx->Nbps == 4) ctx->Nbps = 8;
+
+  ctx->Ntmax = 0;
+  for (unsigned i = 0; i < ctx->No; i++) {
+    if (ctx->Nts[i] == 0) {
+      fprintf(stderr, "Nts[%d] cannot be 0\n", i);
+      fflush(stderr);
+      return 1;
+    }
+    if (ctx->Ntmax < ctx->Nts[i]) ctx->Ntmax = ctx->Nts[i];
+  }
+  for (unsigned i = 0; i < ctx->No; i++) {
+    if (ctx->Ntmax % ctx->Nts[i] != 0) {
+      fprintf(stderr, "Nts[%d] (%u) is not a factor of Ntmax (%u)\n", i, ctx->Nts[i], ctx->Ntmax);
+      fflush(stderr);
+      return 1;
+    }
+  }
+  if (ctx->Nb != 0) {
+    if (((unsigned long long)ctx->Nb * ctx->Ntpb) % ctx->Ntmax != 0) {
+      fprintf(stderr, "Ntmax (%u) is not a factor of Nb*Ntpb (%u * %u = %u)\n", ctx->Ntmax, ctx->Nb,
+              ctx->Ntpb, ctx->Nb * ctx->Ntpb);
+      fflush(stderr);
+      return 1;
+    }
+  } else if (ctx->Ntmax < ctx->Ntpb) {
+    if (ctx->Ntpb % ctx->Ntmax != 0) {
+      fprintf(stderr, "Ntmax (%u) is not a factor of Ntpb (%u)\n", ctx->Ntmax, ctx->Ntpb);
+      fflush(stderr);
+      return 1;
+    }
+    ctx->Nb = 1;
+  } else {
+    if (ctx->Ntmax % ctx->Ntpb != 0) {
+      fprintf(stderr, "Ntpb (%u) is not a factor of Nmax (%u)\n", ctx->Ntpb, ctx->Ntmax);
+      fflush(stderr);
+      return 1;
+    }
+    ctx->Nb = ctx->Ntmax / ctx->Ntpb;
+  }
+  if (ctx->Nb_host == 0 && ctx->h_blkbufs) {
+    fprintf(stderr, "Must specify number of host input blocks when caller-managed\n");
+    fflush(stderr);
+    return 1;
+  } else if (ctx->Nb_host == 0) {
+    ctx->Nb_host = ctx->Nb;
+  }
+  const unsigned long long NbNtpb = (unsigned long long)ctx->Nb * ctx->Ntpb;
+  for (unsigned i = 0; i < ctx->No; i++) {
+    if (ctx->Nas[i] == 0) {
+      fprintf(stderr, "Nas[%d] cannot be 0\n", i);
+      fflush(stderr);
+      return 1;
+    }
+    const unsigned long long ta = (unsigned long long)ctx->Nts[i] * ctx->Nas[i];
+    if (ta < NbNtpb) {
+      if (NbNtpb % ta != 0) {
+        fprintf(stderr, "Nts[%d] * Nas[%d] (%u * %u) must divide Nb * Ntpb (%u * %u)\n", i, i, ctx->Nts[i],
+                ctx->Nas[i], ctx->Nb, ctx->Ntpb);
+        fflush(stderr);
+        return 1;
+      }
+    } else if (ta % NbNtpb != 0) {
+      fprintf(stderr, "Nb * Ntpb (%u * %u) must divide Nts[%d] * Nas[%d] (%u * %u)\n", ctx->Nb, ctx->Ntpb, i, i,
+              ctx->Nts[i], ctx->Nas[i]);
+      fflush(stderr);
+      return 1;
+    }
+  }
+  ctx->Nant = ctx->Nant == 0 ? 1 : ctx->Nant;
+  if (ctx->Nbc == 0) {
+    ctx->Nbc = ctx->Nc;
+  } else {
+    if (ctx->Nbc <= 1) {
+      if (ctx->Nant > 1) {
+        ctx->Nbc = ctx->Nc / ctx->Nant;
+      } else {
+        for (unsigned i = 1; i <= 10; i++)
+          if (ctx->Nc % i == 0) ctx->Nbc = ctx->Nc / i;
+      }
+    }
+    if (ctx->Nbc == 0 || ctx->Nc % ctx->Nbc != 0) {
+      fprintf(stderr, "%d channels cannot be factorised to batches of %d\n", ctx->Nc, ctx->Nbc);
+      return 1;
+    }
+    // Channel batching is accepted for compatibility; all channels are
+    // processed together on the device.
+  }
+
+  // Limits of this implementation.
+  if (ctx->Nc == 0) {
+    fprintf(stderr, "number of coarse channels cannot be zero\n");
+    fflush(stderr);
+    return 1;
+  }
+  for (unsigned i = 0; i < ctx->No; i++) {
+    if (!is_pow2(ctx->Nts[i]) || ilog2u(ctx->Nts[i]) > kMaxLogN) {
+      fprintf(stderr, "Nts[%d] (%u) is not supported: FFT lengths must be powers of two up to 2^%d\n", i,
+              ctx->Nts[i], kMaxLogN);
+      fflush(stderr);
+      return 1;
+    }
+  }
+  if (ctx->incoherently_sum) {
+    if (ctx->Nc % ctx->Nant != 0) {
+      fprintf(stderr, "%d channels cannot be split among %d antennas\n", ctx->Nc, ctx->Nant);
+      fflush(stderr);
+      return 1;
+    }
+    if (!ctx->Aws || !((ctx->Naws == 1 && ctx->Naws < (int)ctx->Nant) || ctx->Naws == (int)ctx->Nant)) {
+      fprintf(stderr, "Not enough antenna-weights provided for the %d antennas: only provided %d.\n", ctx->Nant,
+              ctx->Naws);
+      fflush(stderr);
+      return 1;
+    }
+  }
+
+  for (unsigned i = 0; i < ctx->No; i++) {
+    const unsigned Nss = (unsigned)(NbNtpb / ctx->Nts[i]);
+    ctx->Nds[i] = Nss / ctx->Nas[i];
+    if (ctx->Nds[i] == 0) ctx->Nds[i] = 1;
+    ctx->h_pwrbuf_size[i] = (size_t)abs(ctx->Npolout[i]) * ctx->Nds[i] * ctx->Nts[i] * ctx->Nc * sizeof(float);
+  }
+  return 0;
+}
+
+void derived(const rawspec_context* ctx, int i, unsigned* Nss, unsigned* Nis, unsigned* Nd) {
+  const unsigned long long NbNtpb = (unsigned long long)ctx->Nb * ctx->Ntpb;
+  *Nss = (unsigned)(NbNtpb / ctx->Nts[i]);
+  *Nd = *Nss / ctx->Nas[i];
+  if (*Nd == 0) *Nd = 1;
+  *Nis = ctx->Nas[i] / *Nss;
+  if (*Nis == 0) *Nis = 1;
+}
+
+// ----------------------------------------------------------------------------
+// Host callbacks (run on a CUDA host-function thread; no CUDA calls).
+// ----------------------------------------------------------------------------
+void CUDART_CB pre_dump_fn(void* data) {
+  DumpCb* d = reinterpret_cast<DumpCb*>(data);
+  if (d->ctx->dump_callback) d->ctx->dump_callback(d->ctx, d->product, RAWSPEC_CALLBACK_PRE_DUMP);
+}
+void CUDART_CB post_dump_fn(void* data) {
+  DumpCb* d = reinterpret_cast<DumpCb*>(data);
+  if (d->ctx->dump_callback) d->ctx->dump_callback(d->ctx, d->product, RAWSPEC_CALLBACK_POST_DUMP);
+}
+
+template <typename T>
+int dev_alloc(GpuCtx* g, T** p, size_t bytes) {
+  if (bytes == 0) {
+    *p = nullptr;
+    return 0;
+  }
+  void* v = nullptr;
+  cudaError_t e = cudaMalloc(&v, bytes);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "got error %s allocating %zu bytes of device memory\n", cudaGetErrorName(e), bytes);
+    fflush(stderr);
+    return 1;
+  }
+  g->device_bytes += bytes;
+  *p = reinterpret_cast<T*>(v);
+  return 0;
+}
+
+int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse) {
+  Product& P = g->prod[i];
+  if (!P.large) {
+    SmallLaunch L = P.sl;
+    L.mode = mode;
+    L.inverse = inverse;
+    {
+      ProfScope ps(g, RAWSPEC_GB300_K_SMALL);
+      RSG_CUDA(small_launch(L, g->stream));
+      g->launches++;
+    }
+    if (L.chunks > 1) {
+      FinalizeLaunch F;
+      F.partial = g->d_partial;
+      F.out = P.d_out;
+      F.n_units = L.n_units;
+      F.chunks = L.chunks;
+      F.np = P.np;
+      F.N = P.N;
+      F.Nc = (int)ctx->Nc;
+      F.units_per_chan = L.units_per_chan;
+      F.mode = mode;
+      F.inverse = inverse;
+      ProfScope ps(g, RAWSPEC_GB300_K_FINALIZE);
+      RSG_CUDA(finalize_launch(F, g->stream));
+      g->launches++;
+    }
+  } else {
+    LargeLaunch L = P.ll;
+    L.mode = mode;
+    L.inverse = inverse;
+    {
+      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_A);
+      RSG_CUDA(large_launch_a(L, g->stream));
+      g->launches++;
+    }
+    {
+      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_B);
+      RSG_CUDA(large_launch_b(L, g->stream));
+      g->launches++;
+    }
+    if (L.chunks > 1) {
+      FinalizeLaunch F;
+      F.partial = g->d_partial;
+      F.out = P.d_out;
+      F.n_units = L.n_units;
+      F.chunks = L.chunks;
+      F.np = P.np;
+      F.N = P.N;
+      F.Nc = (int)ctx->Nc;
+      F.units_per_chan = L.units_per_chan;
+      F.mode = mode;
+      F.inverse = inverse;
+      ProfScope ps(g, RAWSPEC_GB300_K_FINALIZE);
+      RSG_CUDA(finalize_launch(F, g->stream));
+      g->launches++;
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ============================================================================
+// Public C interface (the only symbols the library exports).
+// ============================================================================
+#pragma GCC visibility push(default)
+extern "C" {
+
+const char* get_librawspec_version() { return RSG_STR(RAWSPEC_GB300_VERSION) "-gb300"; }
+
+const char* get_cufft_version() { return "none (native sm_103a FFT)"; }
+
+int rawspec_gb300_validate(rawspec_context* ctx) {
+  bool expanded = false;
+  return validate_impl(ctx, &expanded);
+}
+
+int rawspec_gb300_product_info(const rawspec_context* ctx, int product, unsigned* Nss, unsigned* Nis,
+                               unsigned* Nd) {
+  if (!ctx || product < 0 || product >= (int)ctx->No || ctx->Nb == 0 || ctx->Nts[product] == 0 ||
+      ctx->Nas[product] == 0)
+    return 1;
+  unsigned a, b, c;
+  derived(ctx, product, &a, &b, &c);
+  if (Nss) *Nss = a;
+  if (Nis) *Nis = b;
+  if (Nd) *Nd = c;
+  return 0;
+}
+
+int rawspec_initialize(rawspec_context* ctx) {
+  bool expanded = false;
+  if (validate_impl(ctx, &expanded)) return 1;
+  if (ctx->Nbc != ctx->Nc)
+    printf("Batching %d channels into %d batches of %d.\n", ctx->Nc, ctx->Nc / ctx->Nbc, ctx->Nbc);
+
+  for (int i = 0; i < MAX_OUTPUTS; i++) {
+    ctx->h_pwrbuf[i] = nullptr;
+    ctx->h_icsbuf[i] = nullptr;
+  }
+  ctx->gpu_ctx = nullptr;
+
+  cudaError_t rc = cudaSetDevice(ctx->gpu_index);
+  if (rc != cudaSuccess) {
+    fprintf(stderr, "got error %s at %s:%d\n", cudaGetErrorName(rc), __FILE__, __LINE__);
+    fflush(stderr);
+    return 1;
+  }
+  GpuCtx* g = new (std::nothrow) GpuCtx();
+  if (!g) {
+    fprintf(stderr, "unable to allocate rawspec GPU context\n");
+    return 1;
+  }
+  ctx->gpu_ctx = g;
+  g->device = ctx->gpu_index;
+  cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, g->device);
+  for (int i = 0; i < MAX_OUTPUTS; i++) g->cb[i] = {ctx, i};
+  g->fmt = ctx->Nbps == 16 ? FMT_I16 : FMT_I8;
+
+#define FAIL()             \
+  do {                     \
+    rawspec_cleanup(ctx);  \
+    return 1;              \
+  } while (0)
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) {                                                                       \
+      fprintf(stderr, "got error %s at %s:%d\n", cudaGetErrorName(e_), __FILE__, __LINE__);        \
+      fflush(stderr);                                                                              \
+      FAIL();                                                                                      \
+    }                                                                                              \
+  } while (0)
+
+  CK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+
+  const size_t blk_bytes = (size_t)ctx->Ntpb * ctx->Np * ctx->Nc * 2 * (ctx->Nbps / 8);
+  // Host input blocks.
+  if (!ctx->h_blkbufs) {
+    g->caller_managed = false;
+    ctx->h_blkbufs = (char**)calloc(ctx->Nb_host, sizeof(char*));
+    if (!ctx->h_blkbufs) FAIL();
+    for (unsigned i = 0; i < ctx->Nb_host; i++)
+      CK(cudaHostAlloc((void**)&ctx->h_blkbufs[i], blk_bytes, cudaHostAllocWriteCombined));
+  } else {
+    g->caller_managed = true;
+    for (unsigned i = 0; i < ctx->Nb_host; i++) {
+      CK(cudaHostRegister(ctx->h_blkbufs[i], blk_bytes, cudaHostRegisterDefault));
+      g->registered = i + 1;
+    }
+  }
+
+  // Device input buffer.
+  g->in_bytes = blk_bytes * ctx->Nb;
+  if (dev_alloc(g, &g->d_in, g->in_bytes)) FAIL();
+  CK(cudaMemsetAsync(g->d_in, 0, g->in_bytes, g->stream));
+  if (expanded) {
+    g->in4_bytes = g->in_bytes / 2;
+    if (dev_alloc(g, &g->d_in4, g->in4_bytes)) FAIL();
+  }
+
+  // Antenna weights.
+  if (ctx->incoherently_sum) {
+    if (dev_alloc(g, &g->d_aws, ctx->Nant * sizeof(float))) FAIL();
+    std::vector<float> w(ctx->Nant);
+    for (unsigned a = 0; a < ctx->Nant; a++) w[a] = ctx->Naws == 1 ? ctx->Aws[0] : ctx->Aws[a];
+    if (ctx->Naws == 1 && ctx->Nant > 1)
+      printf("Using the single antenna-weight (%f) for all antennas in the incoherent-sum.\n", ctx->Aws[0]);
+    CK(cudaMemcpy(g->d_aws, w.data(), ctx->Nant * sizeof(float), cudaMemcpyHostToDevice));
+  }
+
+  // Products.
+  const int target_ctas = g->sm_count * 4;
+  size_t partial_need = 0, scratch_need = 0;
+  for (unsigned i = 0; i < ctx->No; i++) {
+    Product& P = g->prod[i];
+    P.N = (int)ctx->Nts[i];
+    P.logN = ilog2u(ctx->Nts[i]);
+    P.np = abs(ctx->Npolout[i]);
+    P.Na = ctx->Nas[i];
+    derived(ctx, (int)i, &P.Nss, &P.Nis, &P.Nd);
+    const int pol = P.np == 1 ? POL_TP : ctx->Npolout[i];
+    const int M = (int)(P.Nis > 1 ? P.Nss : P.Na);
+    const int upc = (int)(P.Nis > 1 ? 1 : P.Nss / P.Na);
+
+    CK(cudaHostAlloc((void**)&ctx->h_pwrbuf[i], ctx->h_pwrbuf_size[i], cudaHostAllocDefault));
+    P.out_bytes = ctx->h_pwrbuf_size[i];
+    if (dev_alloc(g, &P.d_out, P.out_bytes)) FAIL();
+    CK(cudaMemsetAsync(P.d_out, 0, P.out_bytes, g->stream));
+    if (ctx->incoherently_sum) {
+      P.ics_bytes = ctx->h_pwrbuf_size[i] / ctx->Nant;
+      CK(cudaHostAlloc((void**)&ctx->h_icsbuf[i], P.ics_bytes, cudaHostAllocDefault));
+      if (dev_alloc(g, &P.d_ics, P.ics_bytes)) FAIL();
+      CK(cudaMemsetAsync(P.d_ics, 0, P.ics_bytes, g->stream));
+    }
+
+    P.large = P.logN > 12;
+    if (!P.large) {
+      SmallLaunch& L = P.sl;
+      L.logN = P.logN;
+      L.fmt = g->fmt;
+      L.nv = (int)ctx->Np;
+      L.pol = pol;
+      L.Nc = (int)ctx->Nc;
+      L.M = M;
+      L.units_per_chan = upc;
+      L.n_units = (int)ctx->Nc * upc;
+      L.chan_stride = (long long)ctx->Nb * ctx->Ntpb;
+      L.in = g->d_in;
+      L.out = P.d_out;
+      L.conj = ctx->input_conjugated ? 1 : 0;
+      size_t pf = 0;
+      if (small_configure(L, target_ctas, &pf)) {
+        fprintf(stderr, "unsupported FFT length %d\n", P.N);
+        FAIL();
+      }
+      partial_need = std::max(partial_need, pf);
+      if (dev_alloc(g, &P.d_tw, (size_t)P.N * sizeof(float2))) FAIL();
+      CK(twiddle_fill(P.d_tw, P.N, P.N, 1, g->stream));
+      L.tw = P.d_tw;
+      CK(small_prepare(L));
+    } else {
+      LargeLaunch& L = P.ll;
+      L.logN = P.logN;
+      L.fmt = g->fmt;
+      L.nv = (int)ctx->Np;
+      L.pol = pol;
+      L.Nc = (int)ctx->Nc;
+      L.Nss = (int)P.Nss;
+      L.M = M;
+      L.units_per_chan = upc;
+      L.n_units = (int)ctx->Nc * upc;
+      L.chan_stride = (long long)ctx->Nb * ctx->Ntpb;
+      L.in = g->d_in;
+      L.out = P.d_out;
+      L.conj = ctx->input_conjugated ? 1 : 0;
+      size_t sf = 0, pf = 0;
+      if (large_configure(L, target_ctas, &sf, &pf)) {
+        fprintf(stderr, "unsupported FFT length %d\n", P.N);
+        FAIL();
+      }
+      scratch_need = std::max(scratch_need, sf);
+      partial_need = std::max(partial_need, pf);
+      const size_t n1 = (size_t)1 << L.logN1, n2 = (size_t)1 << L.logN2;
+      const size_t nlo = (size_t)1 << L.h, nhi = (size_t)1 << (L.logN - L.h);
+      if (dev_alloc(g, &P.d_tw, (n1 + n2 + nlo + nhi) * sizeof(float2))) FAIL();
+      L.twN2 = P.d_tw;
+      L.twN1 = P.d_tw + n2;
+      L.twLo = P.d_tw + n2 + n1;
+      L.twHi = P.d_tw + n2 + n1 + nlo;
+      CK(twiddle_fill(P.d_tw, (long long)n2, (long long)n2, 1, g->stream));
+      CK(twiddle_fill(P.d_tw + n2, (long long)n1, (long long)n1, 1, g->stream));
+      CK(twiddle_fill(P.d_tw + n2 + n1, (long long)nlo, (long long)P.N, 1, g->stream));
+      CK(twiddle_fill(P.d_tw + n2 + n1 + nlo, (long long)nhi, (long long)P.N, (long long)nlo, g->stream));
+      CK(large_prepare(L));
+    }
+  }
+  if (partial_need) {
+    if (dev_alloc(g, &g->d_partial, partial_need * sizeof(float))) FAIL();
+    g->partial_floats = partial_need;
+  }
+  if (scratch_need) {
+    if (dev_alloc(g, &g->d_scratch, scratch_need * sizeof(float2))) FAIL();
+    g->scratch_f2 = scratch_need;
+  }
+  for (unsigned i = 0; i < ctx->No; i++) {
+    g->prod[i].sl.partial = g->d_partial;
+    g->prod[i].ll.partial = g->d_partial;
+    g->prod[i].ll.scratch = g->d_scratch;
+  }
+  CK(cudaStreamSynchronize(g->stream));
+  g->inbuf_count = 0;
+  return 0;
+#undef CK
+#undef FAIL
+}
+
+void rawspec_cleanup(rawspec_context* ctx) {
+  for (int i = 0; i < MAX_OUTPUTS; i++) {
+    if (ctx->h_pwrbuf[i]) {
+      cudaFreeHost(ctx->h_pwrbuf[i]);
+      ctx->h_pwrbuf[i] = nullptr;
+    }
+    if (ctx->h_icsbuf[i]) {
+      cudaFreeHost(ctx->h_icsbuf[i]);
+      ctx->h_icsbuf[i] = nullptr;
+    }
+  }
+  GpuCtx* g = G(ctx);
+  if (!g) return;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  if (g->caller_managed) {
+    for (unsigned i = 0; i < g->registered; i++) cudaHostUnregister(ctx->h_blkbufs[i]);
+  } else if (ctx->h_blkbufs) {
+    for (unsigned i = 0; i < ctx->Nb_host; i++)
+      if (ctx->h_blkbufs[i]) cudaFreeHost(ctx->h_blkbufs[i]);
+    free(ctx->h_blkbufs);
+    ctx->h_blkbufs = nullptr;
+  }
+  cudaFree(g->d_in);
+  cudaFree(g->d_in4);
+  cudaFree(g->d_aws);
+  cudaFree(g->d_partial);
+  cudaFree(g->d_scratch);
+  for (int i = 0; i < MAX_OUTPUTS; i++) {
+    cudaFree(g->prod[i].d_out);
+    cudaFree(g->prod[i].d_ics);
+    cudaFree(g->prod[i].d_tw);
+  }
+  for (auto& p : g->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : g->free_events) cudaEventDestroy(e);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+  ctx->gpu_ctx = nullptr;
+}
+
+int rawspec_copy_blocks_to_gpu(rawspec_context* ctx, off_t src_idx, off_t dst_idx, size_t num_blocks) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  const size_t blk_chan = (size_t)ctx->Ntpb * ctx->Np * 2 * (ctx->Nbps / 8);
+  {
+    ProfScope ps(g, RAWSPEC_GB300_K_H2D);
+    for (size_t b = 0; b < num_blocks; b++) {
+      const off_t sblk = (src_idx + (off_t)b) % ctx->Nb_host;
+      const off_t dblk = (dst_idx + (off_t)b) % ctx->Nb;
+      RSG_CUDA(cudaMemcpy2DAsync((char*)g->d_in + dblk * blk_chan, ctx->Nb * blk_chan, ctx->h_blkbufs[sblk],
+                                 blk_chan, blk_chan, ctx->Nc, cudaMemcpyHostToDevice, g->stream));
+    }
+  }
+  RSG_CUDA(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+int rawspec_copy_blocks_to_gpu_expanding_complex4(rawspec_context* ctx, off_t src_idx, off_t dst_idx,
+                                                  size_t num_blocks) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  if (num_blocks > ctx->Nb) {
+    fprintf(stderr, "%s: num_blocks (%zu) > Nb (%u)\n", __FUNCTION__, num_blocks, ctx->Nb);
+    return 1;
+  }
+  const size_t blk_packed = (size_t)ctx->Ntpb * ctx->Np;  // bytes per channel per block
+  if (!g->d_in4) {
+    g->in4_bytes = g->in_bytes / 2;
+    if (dev_alloc(g, &g->d_in4, g->in4_bytes)) return 1;
+  }
+  {
+    ProfScope ps(g, RAWSPEC_GB300_K_H2D);
+    for (size_t b = 0; b < num_blocks; b++) {
+      const off_t sblk = (src_idx + (off_t)b) % ctx->Nb_host;
+      const off_t dblk = (dst_idx + (off_t)b) % ctx->Nb;
+      RSG_CUDA(cudaMemcpy2DAsync(g->d_in4 + dblk * blk_packed, ctx->Nb * blk_packed, ctx->h_blkbufs[sblk],
+                                 blk_packed, blk_packed, ctx->Nc, cudaMemcpyHostToDevice, g->stream));
+    }
+  }
+  Expand4Launch E;
+  E.packed = g->d_in4;
+  E.out = reinterpret_cast<int8_t*>(g->d_in);
+  E.Nc = (int)ctx->Nc;
+  E.Nb = (int)ctx->Nb;
+  E.blk_bytes_packed = (long long)blk_packed;
+  E.dst_block = (int)(dst_idx % ctx->Nb);
+  E.num_blocks = (int)num_blocks;
+  {
+    ProfScope ps(g, RAWSPEC_GB300_K_EXPAND4);
+    RSG_CUDA(expand4_launch(E, g->stream));
+    g->launches++;
+  }
+  RSG_CUDA(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+int rawspec_zero_blocks_to_gpu(rawspec_context* ctx, off_t dst_idx, size_t num_blocks) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  const size_t blk_chan = (size_t)ctx->Ntpb * ctx->Np * 2 * (ctx->Nbps / 8);
+  for (size_t b = 0; b < num_blocks; b++) {
+    const off_t dblk = (dst_idx + (off_t)b) % ctx->Nb;
+    RSG_CUDA(cudaMemset2DAsync((char*)g->d_in + dblk * blk_chan, ctx->Nb * blk_chan, 0, blk_chan, ctx->Nc,
+                               g->stream));
+  }
+  RSG_CUDA(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+int rawspec_start_processing(rawspec_context* ctx, int fft_dir) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  const int inverse = fft_dir <= 0 ? 1 : 0;
+  g->inbuf_count++;
+  for (unsigned i = 0; i < ctx->No; i++) {
+    Product& P = g->prod[i];
+    const int mode = ((g->inbuf_count - 1) % P.Nis == 0) ? ACC_WRITE : ACC_ADD;
+    if (launch_product(ctx, g, (int)i, mode, inverse)) return 1;
+    if (g->inbuf_count % P.Nis == 0) {
+      if (ctx->incoherently_sum) {
+        IcsLaunch I;
+        I.pwr = P.d_out;
+        I.ics = P.d_ics;
+        I.w = g->d_aws;
+        I.Nd = (int)P.Nd;
+        I.np = P.np;
+        I.Nc = (int)ctx->Nc;
+        I.Nant = (int)ctx->Nant;
+        I.N = P.N;
+        ProfScope ps(g, RAWSPEC_GB300_K_ICS);
+        RSG_CUDA(ics_launch(I, g->stream));
+        g->launches++;
+      }
+      RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
+      {
+        ProfScope ps(g, RAWSPEC_GB300_K_D2H);
+        RSG_CUDA(cudaMemcpyAsync(ctx->h_pwrbuf[i], P.d_out, P.out_bytes, cudaMemcpyDeviceToHost, g->stream));
+        if (ctx->incoherently_sum)
+          RSG_CUDA(cudaMemcpyAsync(ctx->h_icsbuf[i], P.d_ics, P.ics_bytes, cudaMemcpyDeviceToHost, g->stream));
+      }
+      RSG_CUDA(cudaLaunchHostFunc(g->stream, post_dump_fn, &g->cb[i]));
+    }
+  }
+  return 0;
+}
+
+int rawspec_copy_blocks_to_gpu_and_start_processing(rawspec_context* ctx, size_t num_blocks, char expand4bps_to8bps,
+                                                    int fft_dir) {
+  int rc = expand4bps_to8bps ? rawspec_copy_blocks_to_gpu_expanding_complex4(ctx, 0, 0, num_blocks)
+                             : rawspec_copy_blocks_to_gpu(ctx, 0, 0, num_blocks);
+  if (rc) return rc;
+  return rawspec_start_processing(ctx, fft_dir);
+}
+
+int rawspec_reset_integration(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  rawspec_wait_for_completion(ctx);
+  for (unsigned i = 0; i < ctx->No; i++) {
+    RSG_CUDA(cudaMemsetAsync(g->prod[i].d_out, 0, g->prod[i].out_bytes, g->stream));
+    if (g->prod[i].d_ics) RSG_CUDA(cudaMemsetAsync(g->prod[i].d_ics, 0, g->prod[i].ics_bytes, g->stream));
+  }
+  RSG_CUDA(cudaStreamSynchronize(g->stream));
+  g->inbuf_count = 0;
+  return 0;
+}
+
+unsigned int rawspec_check_for_completion(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 0;
+  return cudaStreamQuery(g->stream) == cudaSuccess ? 1u : 0u;
+}
+
+int rawspec_wait_for_completion(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  for (unsigned i = 0; i < ctx->No; i++) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
+  if (cudaStreamSynchronize(g->stream) != cudaSuccess) return 1;
+  if (ctx->exit_soon)
+    fprintf(stderr, "*** rawspec_wait_for_completion detected exit_soon enabled.\n*** Cannot continue!\n");
+  return (int)ctx->exit_soon;
+}
+
+// ---------------------------------------------------------------------------
+// Extensions.
+// ---------------------------------------------------------------------------
+void* rawspec_gb300_stream(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  return g ? (void*)g->stream : nullptr;
+}
+
+void* rawspec_gb300_device_input(rawspec_context* ctx, size_t* bytes) {
+  GpuCtx* g = G(ctx);
+  if (!g) return nullptr;
+  if (bytes) *bytes = g->in_bytes;
+  return g->d_in;
+}
+
+int rawspec_gb300_set_profiling(rawspec_context* ctx, int enable) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  g->profiling = enable != 0;
+  return 0;
+}
+
+int rawspec_gb300_profile(rawspec_context* ctx, int kernel_class, double* total_ms, unsigned long long* launches) {
+  GpuCtx* g = G(ctx);
+  if (!g || kernel_class < 0 || kernel_class >= RAWSPEC_GB300_K_COUNT) return 1;
+  if (cudaStreamSynchronize(g->stream) != cudaSuccess) return 1;
+  collect_profile(g);
+  if (total_ms) *total_ms = g->prof_ms[kernel_class];
+  if (launches) *launches = g->prof_n[kernel_class];
+  return 0;
+}
+
+int rawspec_gb300_reset_profile(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  if (cudaStreamSynchronize(g->stream) != cudaSuccess) return 1;
+  collect_profile(g);
+  for (int k = 0; k < RAWSPEC_GB300_K_COUNT; k++) {
+    g->prof_ms[k] = 0;
+    g->prof_n[k] = 0;
+  }
+  return 0;
+}
+
+unsigned long long rawspec_gb300_kernel_launches(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  return g ? g->launches : 0;
+}
+
+size_t rawspec_gb300_device_bytes(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  return g ? g->device_bytes : 0;
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

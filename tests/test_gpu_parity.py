@@ -1,0 +1,204 @@
+"""Parity of the native CUDA path (through the C-ABI) with the FP64 oracle.
+
+Small configurations are compared bin by bin with the committed golden
+fixtures and with the oracle run on the fly; full-size configurations are
+checked through size-independent properties (Parseval per integration, the
+Stokes identities between modes)."""
+import ctypes as C
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from cases import CASES, derived_nb
+from oracle import oracle as O
+from rawspec_gb300 import api, synth
+from util import REL_TOL, load_golden, normalized_error
+
+pytestmark = pytest.mark.gpu
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def run_gpu(c, blocks, weights=None, fft_dir=None, Nbc=0):
+    spec = api.Spectrometer(c["Nc"], c["Np"], c["Ntpb"], c["nbits"], c["products"], Nant=c.get("Nant", 1),
+                            conj=c["conj"], weights=None if weights is None else list(weights), Nbc=Nbc)
+    try:
+        spec.process(blocks, fft_dir=c["fft_dir"] if fft_dir is None else fft_dir)
+        return [np.array(d) for d in spec.dumps], [np.array(s) for s in spec.ics], spec.events, spec.kernel_launches()
+    finally:
+        spec.close()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_golden_parity(cuda_device, name):
+    c = CASES[name]
+    g = load_golden(name)
+    dumps, ics, _, launches = run_gpu(c, g["blocks"], g.get("weights"))
+    assert launches > 0
+    for i, (nt, na, npol) in enumerate(c["products"]):
+        ref = g[f"out{i}"]
+        assert dumps[i].shape == ref.shape, (i, dumps[i].shape, ref.shape)
+        err = normalized_error(dumps[i], ref, npol, c["Nc"], nt)
+        assert err < REL_TOL, (name, i, err)
+        if c.get("ics"):
+            eri = normalized_error(ics[i], g[f"ics{i}"], npol, c["Nc"] // c["Nant"], nt)
+            assert eri < REL_TOL, (name, i, "ics", eri)
+
+
+def oracle_for(c, blocks, weights=None, inverse=None):
+    cfg = O.make_cfg(c["Nc"], c["Np"], c["Ntpb"], derived_nb(c), c["nbits"], c["products"], Nant=c.get("Nant", 1),
+                     conj=c["conj"], inverse=(1 if c["fft_dir"] <= 0 else 0) if inverse is None else inverse,
+                     weights=weights)
+    return O.run_oracle(cfg, blocks)
+
+
+@pytest.mark.parametrize("logn", list(range(0, 13)))
+@pytest.mark.parametrize("npol", [1, 4, -4])
+def test_small_lengths_all_modes(cuda_device, logn, npol):
+    nt = 1 << logn
+    Ntpb = max(4096, nt)
+    # Na chosen so that some integrations stay within the buffer (Nd > 1),
+    # and large enough that one unit is split over several CTAs.
+    na = max(1, min(64, (2 * Ntpb) // nt // 2))
+    c = dict(Nc=3, Np=2, Ntpb=Ntpb, nbits=8, nblocks=2, products=[(nt, na, npol)], conj=1, fft_dir=1)
+    blocks = synth.gaussian_blocks(2, 3, Ntpb, 2, sigma=18.0, seed=100 + logn)
+    dumps, _, _, _ = run_gpu(c, blocks)
+    ref, _ = oracle_for(c, blocks)
+    err = normalized_error(dumps[0], ref[0], npol, 3, nt)
+    assert err < REL_TOL, (nt, npol, err)
+
+
+@pytest.mark.parametrize("logn", [13, 14, 16, 18, 20])
+def test_large_lengths(cuda_device, logn):
+    nt = 1 << logn
+    c = dict(Nc=1, Np=2, Ntpb=nt // 2, nbits=8, nblocks=4, products=[(nt, 2, 4)], conj=0, fft_dir=1)
+    blocks = synth.gaussian_blocks(4, 1, nt // 2, 2, sigma=16.0, seed=200 + logn)
+    dumps, _, _, _ = run_gpu(c, blocks)
+    ref, _ = oracle_for(c, blocks)
+    err = normalized_error(dumps[0], ref[0], 4, 1, nt)
+    assert err < REL_TOL, (nt, err)
+
+
+def test_inverse_direction_and_nis_chunks(cuda_device):
+    c = dict(Nc=4, Np=2, Ntpb=8192, nbits=8, nblocks=6, products=[(1024, 24, -4), (8192, 3, 1)], conj=1, fft_dir=-1)
+    blocks = synth.gaussian_blocks(6, 4, 8192, 2, sigma=20.0, seed=7)
+    dumps, _, events, _ = run_gpu(c, blocks)
+    ref, _ = oracle_for(c, blocks)
+    for i, (nt, na, npol) in enumerate(c["products"]):
+        assert dumps[i].shape == ref[i].shape
+        assert normalized_error(dumps[i], ref[i], npol, 4, nt) < REL_TOL
+
+
+def test_dump_callbacks_are_ordered(cuda_device):
+    c = dict(Nc=2, Np=2, Ntpb=1024, nbits=8, nblocks=6, products=[(256, 8, 1), (64, 32, 4)], conj=0, fft_dir=1)
+    blocks = synth.gaussian_blocks(6, 2, 1024, 2, seed=9)
+    dumps, _, events, _ = run_gpu(c, blocks)
+    # product 0: Nis = 2 -> 3 dumps in 6 buffers; product 1: Nis = 2 -> 3 dumps
+    assert len(dumps[0]) == 3 and len(dumps[1]) == 3
+    for prod in (0, 1):
+        seq = [k for p, k in events if p == prod]
+        # every POST is directly preceded by its PRE
+        for j, k in enumerate(seq):
+            if k == api.RAWSPEC_CALLBACK_POST_DUMP:
+                assert j > 0 and seq[j - 1] == api.RAWSPEC_CALLBACK_PRE_DUMP
+        assert seq.count(api.RAWSPEC_CALLBACK_POST_DUMP) == 3
+
+
+def test_reset_zero_and_completion(cuda_device):
+    lib = api.load_library()
+    spec = api.Spectrometer(2, 2, 1024, 8, [(256, 8, 1)])
+    try:
+        blocks = synth.gaussian_blocks(1, 2, 1024, 2, seed=3)
+        spec.load_blocks(blocks)
+        spec.copy_to_gpu()
+        spec.start()
+        assert spec.wait() == 0
+        assert lib.rawspec_check_for_completion(C.byref(spec.ctx)) == 1
+        # zeroed input gives an all-zero integration after a reset
+        assert lib.rawspec_reset_integration(C.byref(spec.ctx)) == 0
+        assert lib.rawspec_zero_blocks_to_gpu(C.byref(spec.ctx), 0, 1) == 0
+        for _ in range(8):
+            spec.start()
+        assert spec.wait() == 0
+        assert len(spec.dumps[0]) == 2
+        assert np.all(spec.dumps[0][-1] == 0)
+        assert np.any(spec.dumps[0][0] != 0)
+    finally:
+        spec.close()
+
+
+def test_exit_soon_is_returned(cuda_device):
+    spec = api.Spectrometer(2, 2, 1024, 8, [(256, 4, 1)])
+    try:
+        spec.ctx.exit_soon = 1
+        assert spec.wait() == 1
+    finally:
+        spec.close()
+
+
+def _parseval_check(nt, na, blocks, Nc, Ntpb, dumps, npol):
+    """Sum over fine channels of each integrated spectrum equals Nt times the
+    voltage power of the integration's samples (size-independent property)."""
+    x = blocks.view(np.int8).reshape(-1, Nc, Ntpb, 2, 2).astype(np.float64)
+    x = np.maximum(x, -127) / 127.0
+    x = np.transpose(x, (1, 0, 2, 3, 4)).reshape(Nc, -1, 2, 2)  # [c][t][pol][ri]
+    p = (x ** 2).sum(axis=(2, 3)) if npol != 4 else (x ** 2).sum(axis=3)  # [c][t] or [c][t][pol]
+    nint = p.shape[1] // (nt * na)
+    if npol == 4:
+        want = p[:, : nint * nt * na].reshape(Nc, nint, nt * na, 2).sum(axis=2) * nt  # [c][d][pol]
+        got = dumps.reshape(nint, 4, Nc, nt)[:, :2].sum(axis=-1)                    # [d][pol][c]
+        got = np.transpose(got, (2, 0, 1))
+    else:
+        want = p[:, : nint * nt * na].reshape(Nc, nint, nt * na).sum(axis=2) * nt
+        got = dumps.reshape(nint, abs(npol), Nc, nt)[:, 0].sum(axis=-1).T
+    np.testing.assert_allclose(got, want, rtol=1e-5)
+
+
+@pytest.mark.parametrize("npol", [1, 4])
+def test_full_size_production_shape_parseval(cuda_device, npol):
+    # 64 channels, Ntpb 524288 (128 MiB blocks), one 2-block buffer; the
+    # products of the production configuration with integration lengths
+    # that dump within the buffer.
+    Nc, Ntpb = 64, 524288
+    blocks = synth.gaussian_blocks(2, Nc, Ntpb, 2, sigma=20.0, seed=21)
+    prods = [(1 << 20, 1, npol), (8, 128, npol), (1024, 1024, npol)]
+    c = dict(Nc=Nc, Np=2, Ntpb=Ntpb, nbits=8, products=prods, conj=0, fft_dir=1)
+    dumps, _, _, _ = run_gpu(c, blocks)
+    for i, (nt, na, _) in enumerate(prods):
+        assert len(dumps[i]) == 1
+        _parseval_check(nt, na, blocks, Nc, Ntpb, dumps[i][0], npol)
+
+
+def test_full_size_stokes_identities(cuda_device):
+    Nc, Ntpb = 64, 524288
+    blocks = synth.gaussian_blocks(2, Nc, Ntpb, 2, sigma=20.0, seed=22)
+    base = dict(Nc=Nc, Np=2, Ntpb=Ntpb, nbits=8, conj=1, fft_dir=1)
+    full, _, _, _ = run_gpu(dict(base, products=[(1 << 20, 1, 4), (1024, 1024, 4)]), blocks)
+    stokes, _, _, _ = run_gpu(dict(base, products=[(1 << 20, 1, -4), (1024, 1024, -4)]), blocks)
+    for i, nt in enumerate([1 << 20, 1024]):
+        F = full[i][0].reshape(4, Nc, nt).astype(np.float64)
+        S = stokes[i][0].reshape(4, Nc, nt).astype(np.float64)
+        scale = S[0]
+        assert np.max(np.abs(S[0] - (F[0] + F[1])) / scale) < 1e-6
+        assert np.max(np.abs(S[1] - (F[0] - F[1])) / scale) < 1e-6
+        assert np.max(np.abs(S[2] - F[2]) / scale) < 1e-6
+        assert np.max(np.abs(S[3] - F[3]) / scale) < 1e-6
+
+
+def test_unpack_matches_texture_unit(cuda_device, tmp_path):
+    so = tmp_path / "libsnorm_probe.so"
+    cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-shared", "-Xcompiler",
+           "-fPIC", f"-I{ROOT / 'rawspec_gb300' / 'csrc'}", "-o", str(so), str(ROOT / "tests" / "probe" / "snorm_probe.cu")]
+    subprocess.run(cmd, check=True)
+    lib = C.CDLL(str(so))
+    t8, o8 = np.zeros(256, np.float32), np.zeros(256, np.float32)
+    t16, o16 = np.zeros(65536, np.float32), np.zeros(65536, np.float32)
+    fp = C.POINTER(C.c_float)
+    rc = lib.snorm_probe(t8.ctypes.data_as(fp), o8.ctypes.data_as(fp), t16.ctypes.data_as(fp), o16.ctypes.data_as(fp))
+    assert rc == 0
+    assert np.array_equal(t8.view(np.uint32), o8.view(np.uint32)), np.nonzero(t8 != o8)
+    assert np.array_equal(t16.view(np.uint32), o16.view(np.uint32)), np.nonzero(t16 != o16)
+    # and the oracle's unpack agrees with both
+    assert all(float(o8[i]) == O.snorm(int(np.int8(np.uint8(i))), 8) for i in range(256))
