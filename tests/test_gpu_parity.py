@@ -108,7 +108,8 @@ def test_dump_callbacks_are_ordered(cuda_device):
 
 def test_reset_zero_and_completion(cuda_device):
     lib = api.load_library()
-    spec = api.Spectrometer(2, 2, 1024, 8, [(256, 8, 1)])
+    # Nt 256, Na 4, Ntpb 1024: one integration (one dump) per buffer
+    spec = api.Spectrometer(2, 2, 1024, 8, [(256, 4, 1)])
     try:
         blocks = synth.gaussian_blocks(1, 2, 1024, 2, seed=3)
         spec.load_blocks(blocks)
@@ -116,15 +117,35 @@ def test_reset_zero_and_completion(cuda_device):
         spec.start()
         assert spec.wait() == 0
         assert lib.rawspec_check_for_completion(C.byref(spec.ctx)) == 1
-        # zeroed input gives an all-zero integration after a reset
+        assert len(spec.dumps[0]) == 1 and np.all(spec.dumps[0][0] > 0)
+        # zeroed input gives all-zero integrations after a reset
         assert lib.rawspec_reset_integration(C.byref(spec.ctx)) == 0
         assert lib.rawspec_zero_blocks_to_gpu(C.byref(spec.ctx), 0, 1) == 0
         for _ in range(8):
             spec.start()
         assert spec.wait() == 0
-        assert len(spec.dumps[0]) == 2
-        assert np.all(spec.dumps[0][-1] == 0)
-        assert np.any(spec.dumps[0][0] != 0)
+        assert len(spec.dumps[0]) == 9
+        assert all(np.all(d == 0) for d in spec.dumps[0][1:])
+    finally:
+        spec.close()
+
+
+def test_reset_restarts_multi_buffer_integration(cuda_device):
+    # Nt 256, Na 8, Ntpb 1024: Nis = 2 buffers per dump; a reset in the middle
+    # of an integration discards the partial sum.
+    c = dict(Nc=2, Np=2, Ntpb=1024, nbits=8, nblocks=2, products=[(256, 8, 1)], conj=0, fft_dir=1)
+    blocks = synth.gaussian_blocks(2, 2, 1024, 2, seed=4)
+    lib = api.load_library()
+    spec = api.Spectrometer(2, 2, 1024, 8, [(256, 8, 1)])
+    try:
+        spec.load_blocks(blocks[:1])
+        spec.copy_to_gpu()
+        spec.start()                      # half an integration of block 0
+        assert lib.rawspec_reset_integration(C.byref(spec.ctx)) == 0
+        spec.process(blocks)              # blocks 0 and 1 -> one dump
+        assert len(spec.dumps[0]) == 1
+        ref, _ = oracle_for(c, blocks)
+        assert normalized_error(np.array(spec.dumps[0]), ref[0], 1, 2, 256) < REL_TOL
     finally:
         spec.close()
 
