@@ -277,7 +277,8 @@ def run_native(args, rank, world, local_rank):
         dom_name = f"k_{dom}"
         t_ms, n = prof[dom]
     achieved = alg / (t_ms / max(n, 1) / 1e3) / 1e9 if n else None
-    traffic = load_traffic().get(dom_name.split()[0])
+    tr = load_traffic()
+    traffic = tr.get("k_large_a+k_large_b") if dom in ("large_a", "large_b") else tr.get(dom_name)
     line = {
         "metric": "RAW-in GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
