@@ -61,6 +61,45 @@ unsigned long long rawspec_gb300_kernel_launches(rawspec_context *ctx);
 /* Bytes of device memory held by the context. */
 size_t rawspec_gb300_device_bytes(rawspec_context *ctx);
 
+/* Allocation-free computation of one output product for one device-resident
+ * input buffer.  No counterpart in the reference library.
+ *
+ * For callers that cannot allocate device memory: a streaming pipeline thread
+ * that must never stall (cudaMalloc and cudaFree synchronise the whole device,
+ * blocking every other stream), or a host framework that hands out all device
+ * memory from its own pool and budget.  The caller passes the input and the
+ * output; the function calls no cudaMalloc, cudaFree or other allocating
+ * routine and needs no rawspec_initialize().
+ *
+ *   d_in     device input, [Nc][samples_per_channel][Np][re,im], Nbps = 8 or
+ *            16 bits per component (the layout rawspec_copy_blocks_to_gpu
+ *            produces; 4-bit input must be expanded first)
+ *   Nt, Na   FFT length (power of two, at most 4096) and spectra per
+ *            integration; Nt*Na must divide samples_per_channel
+ *   Npolout  1, +4 (full pol) or -4 (Stokes), coerced to 1 unless Np == 2
+ *   d_out    device output, [Nd][|Npolout|][Nc][Nt] float, FFT-shifted, with
+ *            Nd = samples_per_channel / (Nt*Na): the same values
+ *            rawspec_start_processing() dumps for such a product
+ *   stream   cudaStream_t to queue the work on (0 = legacy default stream)
+ *
+ * Scratch: a file-scope device array of 4 MiB of partial sums plus a 4096-entry
+ * twiddle table (4.03 MiB), held by every GPU that loads the library until the
+ * process exits.  The partial-sum split is limited to what fits; FFT lengths
+ * above 4096 are rejected with an error.  The first call on a device looks up
+ * the array's device address (make that first call before any stream capture
+ * on that device).  Every call shares the array and it keeps the last call's
+ * contents; everything a call reads from it is written by the same call first.
+ * Calls that overlap on the GPU (different streams, or another host thread)
+ * race on the array and must be serialised by the caller.
+ * Returns 0 when the work is queued, 1 on invalid arguments or a CUDA error
+ * (message on stderr). */
+int rawspec_gb300_product_noalloc(const void *d_in, unsigned int Nc, unsigned int Np,
+                                  unsigned int Nbps,
+                                  unsigned long long samples_per_channel,
+                                  unsigned int Nt, unsigned int Na, int Npolout,
+                                  int fft_dir, int input_conjugated,
+                                  float *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
