@@ -19,13 +19,14 @@ namespace rsg {
 // the reference gives its FFT input (rawspec_gpu.cu:1454-1460).
 // ----------------------------------------------------------------------------
 
-// Integer -> float conversion of one component.  The reference reads the
-// input through a CUDA texture in cudaReadModeNormalizedFloat
-// (rawspec_gpu.cu:133-148, :845-866), which maps a signed n-bit code x to
-// x / (2^(n-1) - 1), clamped to -1.0 for the most negative code.  We compute
-// the correctly rounded quotient with one multiply and one FMA-based
-// correction step, which is exact for every 8- and 16-bit code (checked
-// exhaustively) and matches the texture unit bit for bit (GPU probe test).
+// Integer -> float conversion of one component as the reference performs it.
+// The reference reads the input through a CUDA texture in
+// cudaReadModeNormalizedFloat (rawspec_gpu.cu:133-148, :845-866), which maps a
+// signed n-bit code x to x / (2^(n-1) - 1), clamped to -1.0 for the most
+// negative code.  snorm() computes the correctly rounded quotient with one
+// multiply and one FMA-based correction step, which is exact for every 8- and
+// 16-bit code (checked exhaustively) and matches the texture unit bit for bit
+// (GPU probe test).  The kernels use the equivalent integer form below.
 template <int D>
 __device__ __forceinline__ float snorm(int x) {
   constexpr float d = (float)D;
@@ -44,21 +45,46 @@ template <> struct SampleWord<FMT_I8, 1> { using type = uint16_t; };
 template <> struct SampleWord<FMT_I16, 2> { using type = uint2; };
 template <> struct SampleWord<FMT_I16, 1> { using type = uint32_t; };
 
-// Conversion of a loaded sample word into NP complex floats.
-__device__ __forceinline__ void unpack_word(uint32_t w, float2 (&o)[2]) {
-  o[0] = make_float2(snorm<127>((int)(int8_t)(w & 0xff)), snorm<127>((int)(int8_t)((w >> 8) & 0xff)));
-  o[1] = make_float2(snorm<127>((int)(int8_t)((w >> 16) & 0xff)), snorm<127>((int)(int8_t)(w >> 24)));
+// Integer unpack used by the kernels: the exact integer codes as floats, with
+// the most negative code clamped like the texture's SNORM mapping (-128 ->
+// -127, -32768 -> -32767) and the 1/127 (1/32767) SNORM scale left out.
+// Every detected product is quadratic in the samples, so the kernels apply
+// the scale once, as 1/127^2 (1/32767^2), to the integrated results.  The
+// codes themselves (and the 4-bit nibble expansion) are bit-exact.
+__device__ __forceinline__ void unpack_word_int(uint32_t w, float2 (&o)[2]) {
+  w = __vmaxs4(w, 0x81818181u);
+  o[0] = make_float2((float)(int8_t)(w & 0xff), (float)(int8_t)((w >> 8) & 0xff));
+  o[1] = make_float2((float)(int8_t)((w >> 16) & 0xff), (float)(int8_t)(w >> 24));
 }
-__device__ __forceinline__ void unpack_word(uint16_t w, float2 (&o)[1]) {
-  o[0] = make_float2(snorm<127>((int)(int8_t)(w & 0xff)), snorm<127>((int)(int8_t)(w >> 8)));
+__device__ __forceinline__ void unpack_word_int(uint16_t w16, float2 (&o)[1]) {
+  const uint32_t w = __vmaxs4((uint32_t)w16, 0x81818181u);
+  o[0] = make_float2((float)(int8_t)(w & 0xff), (float)(int8_t)((w >> 8) & 0xff));
 }
-__device__ __forceinline__ void unpack_word(uint2 w, float2 (&o)[2]) {
-  o[0] = make_float2(snorm<32767>((int)(int16_t)(w.x & 0xffff)), snorm<32767>((int)(int16_t)(w.x >> 16)));
-  o[1] = make_float2(snorm<32767>((int)(int16_t)(w.y & 0xffff)), snorm<32767>((int)(int16_t)(w.y >> 16)));
+__device__ __forceinline__ void unpack_word_int(uint2 w, float2 (&o)[2]) {
+  const uint32_t a = __vmaxs2(w.x, 0x80018001u), b = __vmaxs2(w.y, 0x80018001u);
+  o[0] = make_float2((float)(int16_t)(a & 0xffff), (float)(int16_t)(a >> 16));
+  o[1] = make_float2((float)(int16_t)(b & 0xffff), (float)(int16_t)(b >> 16));
 }
-__device__ __forceinline__ void unpack_word(uint32_t w, float2 (&o)[1]) {
-  o[0] = make_float2(snorm<32767>((int)(int16_t)(w & 0xffff)), snorm<32767>((int)(int16_t)(w >> 16)));
+__device__ __forceinline__ void unpack_word_int(uint32_t w, float2 (&o)[1], int /*int16 tag*/) {
+  const uint32_t a = __vmaxs2(w, 0x80018001u);
+  o[0] = make_float2((float)(int16_t)(a & 0xffff), (float)(int16_t)(a >> 16));
 }
+
+// Loads-and-unpacks one sample word of format FMT with NP polarisations.
+template <int FMT, int NP>
+struct Unpack;
+template <> struct Unpack<FMT_I8, 2> {
+  static __device__ __forceinline__ void run(uint32_t w, float2 (&o)[2]) { unpack_word_int(w, o); }
+};
+template <> struct Unpack<FMT_I8, 1> {
+  static __device__ __forceinline__ void run(uint16_t w, float2 (&o)[1]) { unpack_word_int(w, o); }
+};
+template <> struct Unpack<FMT_I16, 2> {
+  static __device__ __forceinline__ void run(uint2 w, float2 (&o)[2]) { unpack_word_int(w, o); }
+};
+template <> struct Unpack<FMT_I16, 1> {
+  static __device__ __forceinline__ void run(uint32_t w, float2 (&o)[1]) { unpack_word_int(w, o, 16); }
+};
 
 // ----------------------------------------------------------------------------
 // Complex helpers.
@@ -70,7 +96,8 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 w) {
   return make_float2(__fmaf_rn(a.x, w.x, -a.y * w.y), __fmaf_rn(a.x, w.y, a.y * w.x));
 }
 
-// cos(pi t / 16) for t in [0, 16], as exact decimal literals.
+// cos(pi t / 16) for t in [0, 16], as decimal literals (non-recursive, so a
+// constant argument always folds).
 __host__ __device__ constexpr double cos_pi16(int t) {
   return t == 0 ? 1.0
        : t == 1 ? 0.98078528040323043
@@ -81,7 +108,14 @@ __host__ __device__ constexpr double cos_pi16(int t) {
        : t == 6 ? 0.38268343236508984
        : t == 7 ? 0.19509032201612833
        : t == 8 ? 0.0
-       : -cos_pi16(16 - t);
+       : t == 9 ? -0.19509032201612833
+       : t == 10 ? -0.38268343236508984
+       : t == 11 ? -0.55557023301960229
+       : t == 12 ? -0.70710678118654757
+       : t == 13 ? -0.83146961230254524
+       : t == 14 ? -0.92387953251128674
+       : t == 15 ? -0.98078528040323043
+       : -1.0;
 }
 // sin(pi t / 16) for t in [0, 16).
 __host__ __device__ constexpr double sin_pi16(int t) {

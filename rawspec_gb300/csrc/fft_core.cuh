@@ -98,8 +98,33 @@ struct FftShape {
   static constexpr int PASSES = FULL + (RLAST > 1 ? 1 : 0);
 };
 
-// Group FFT.  tw: table of W_N^m = exp(-2 pi i m / N), m in [0, N), in shared
-// (or global) memory.  sm: this group's exchange buffers, NV buffers of
+// Twiddle table of a GroupFFT<N, R>, one block per twiddled pass, laid out so
+// that the lanes of a warp read consecutive (or identical) entries:
+//   full pass p >= 1 (Ns = R^p):    [r-1][k]  = W_N^(k r N/(Ns R)), k < Ns
+//   trailing pass (radix RL):       [r-1][b]  = W_N^(b r),          b < N/RL
+// StockhamTw<N, R>::offset(p) is the start of pass p's block; `size` the total.
+__host__ __device__ constexpr int stockham_tw_offset(int N, int R, int p) {
+  // blocks of passes 1 .. p-1
+  int off = 0, Ns = R;
+  for (int q = 1; q < p; ++q) {
+    off += (R - 1) * Ns;
+    Ns *= R;
+  }
+  return off;
+}
+__host__ __device__ constexpr int stockham_tw_size(int N, int R) {
+  if (R <= 1 || N <= R) return 0;
+  int full = 0, Ns = 1;
+  while (Ns * R <= N) {
+    Ns *= R;
+    ++full;
+  }
+  const int rl = N / Ns;
+  return stockham_tw_offset(N, R, full) + (rl > 1 ? (rl - 1) * (N / rl) : 0);
+}
+
+// Group FFT.  tw: the pass-ordered twiddle table described above (shared or
+// global memory).  sm: this group's exchange buffers, NV buffers of
 // smem_padded_len(N) float2 each, spaced by `sm_stride` float2.  SYNC is a
 // functor performing the barrier required between the group's threads.
 template <int N, int R, int NV>
@@ -121,10 +146,10 @@ struct GroupFFT {
         // Twiddles (identity on the first pass).
         if (p > 0) {
           const int k = j & (Ns - 1);
-          const int step = N / (Ns * R);  // tw index of element r is k*r*step
+          const float2* twp = tw + stockham_tw_offset(N, R, p) + k;
 #pragma unroll
           for (int r = 1; r < R; ++r) {
-            const float2 w = tw[k * r * step];
+            const float2 w = twp[(r - 1) * Ns];
 #pragma unroll
             for (int q = 0; q < NV; ++q) v[q][r] = cmul(v[q][r], w);
           }
@@ -164,12 +189,14 @@ struct GroupFFT {
         // butterflies b = j + q*T on elements m = q + r*Q.
         constexpr int RL = S::RLAST;
         constexpr int Q = R / RL;
+        constexpr int NSL = N / RL;
+        const float2* twl = tw + stockham_tw_offset(N, R, S::FULL) + j;
 #pragma unroll
         for (int qb = 0; qb < Q; ++qb) {
-          const int b = j + qb * T;  // k = b (b < Ns); tw index b*r
+          // butterfly b = j + qb*T; its twiddles W_N^(b r) sit at [r-1][b]
 #pragma unroll
           for (int r = 1; r < RL; ++r) {
-            const float2 w = tw[b * r];
+            const float2 w = twl[(r - 1) * NSL + qb * T];
 #pragma unroll
             for (int q = 0; q < NV; ++q) v[q][qb + r * Q] = cmul(v[q][qb + r * Q], w);
           }

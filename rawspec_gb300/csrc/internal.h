@@ -44,6 +44,7 @@ struct SmallLaunch {
   const float2* tw = nullptr; // W_N^m, m < N
   // per call
   int mode = ACC_WRITE, inverse = 0, conj = 0;
+  float scale = 1.0f;         // SNORM scale squared, applied to the results
 };
 
 // Chooses block size, units per block and chunks per unit.  target_ctas is
@@ -61,6 +62,7 @@ struct FinalizeLaunch {
   float* out = nullptr;
   int n_units = 0, chunks = 0, np = 1, N = 0, Nc = 0, units_per_chan = 0;
   int mode = ACC_WRITE, inverse = 0;
+  float scale = 1.0f;
 };
 cudaError_t finalize_launch(const FinalizeLaunch& L, cudaStream_t s);
 
@@ -81,14 +83,23 @@ struct LargeLaunch {
   float2* scratch = nullptr;      // [Nc*Nss][nv][N2][N1]
   float* out = nullptr;
   float* partial = nullptr;
-  const float2* twN2 = nullptr;   // W_N2^m
-  const float2* twN1 = nullptr;   // W_N1^m
+  const float2* twN2 = nullptr;   // pass-ordered Stockham table of the N2-point FFT
+  const float2* twN1 = nullptr;   // pass-ordered Stockham table of the N1-point FFT
   const float2* twLo = nullptr;   // W_N^i, i < 2^h
   const float2* twHi = nullptr;   // W_N^(i*2^h), i < N / 2^h
+  const float2* twM = nullptr;    // [m][n1] = W_N^(n1*m*T2), m < R_A, the pass-A output twiddles
   int h = 0;
   int mode = ACC_WRITE, inverse = 0, conj = 0;
+  float scale = 1.0f;
 };
 int large_configure(LargeLaunch& L, int target_ctas, size_t* scratch_float2, size_t* partial_floats);
+// Radix of pass A (values per thread of its N2-point FFT) and its threads per
+// column FFT, which define the pass-A twiddle table twM ([R_A][N1]).
+int large_pass_a_radix();
+// Sizes (entries) of the pass-ordered twiddle tables.
+int stockham_table_size(int N, int R);
+int small_radix(int logN, int pol);
+int large_pass_b_radix(int pol);
 cudaError_t large_launch_a(const LargeLaunch& L, cudaStream_t s);
 cudaError_t large_launch_b(const LargeLaunch& L, cudaStream_t s);
 // Raises both kernels' dynamic shared-memory limits on the current device.
@@ -100,6 +111,10 @@ cudaError_t large_prepare(const LargeLaunch& L);
 // W_n^m = exp(-2 pi i m stride / n) for m < count, computed in FP64 with
 // sincospi and rounded to float.
 cudaError_t twiddle_fill(float2* dst, long long count, long long n, long long stride, cudaStream_t s);
+// Pass-ordered Stockham table of an N-point GroupFFT of radix R.
+cudaError_t stockham_twiddle_fill(float2* dst, int N, int R, cudaStream_t s);
+// dst[m*N1 + n1] = W_N^((n1*m*T) mod N) for m < R, n1 < N1.
+cudaError_t passa_twiddle_fill(float2* dst, int N1, int R, long long T, long long N, cudaStream_t s);
 
 // 4-bit complex expansion: for each of num_blocks blocks and each channel,
 // bytes of the packed staging buffer become (re, im) int8 pairs in the input

@@ -25,6 +25,55 @@ cudaError_t twiddle_fill(float2* dst, long long count, long long n, long long st
   return cudaGetLastError();
 }
 
+__device__ __forceinline__ float2 w_of(long long e, long long n) {
+  double s, c;
+  sincospi(2.0 * (double)e / (double)n, &s, &c);
+  return make_float2((float)c, (float)(-s));
+}
+
+// Pass-ordered twiddle table of a GroupFFT<N, R> (layout in fft_core.cuh):
+// full passes p >= 1 with Ns = R^p hold [r-1][k] = W_N^(k r N/(Ns R)); the
+// trailing pass of radix RL holds [r-1][b] = W_N^(b r).
+__global__ void k_stockham_twiddle(float2* dst, int N, int R, int size) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= size) return;
+  int off = 0, Ns = R;
+  while (Ns * R <= N) {  // full passes 1 .. FULL-1
+    const int blk = (R - 1) * Ns;
+    if (i < off + blk) {
+      const int r = (i - off) / Ns + 1, k = (i - off) % Ns;
+      dst[i] = w_of((long long)k * r * (N / (Ns * R)), N);
+      return;
+    }
+    off += blk;
+    Ns *= R;
+  }
+  const int rl = N / Ns;  // trailing pass
+  const int nsl = N / rl;
+  const int r = (i - off) / nsl + 1, b = (i - off) % nsl;
+  dst[i] = w_of((long long)b * r, N);
+}
+
+cudaError_t stockham_twiddle_fill(float2* dst, int N, int R, cudaStream_t s) {
+  const int size = stockham_table_size(N, R);
+  if (size <= 0) return cudaSuccess;
+  k_stockham_twiddle<<<(size + 255) / 256, 256, 0, s>>>(dst, N, R, size);
+  return cudaGetLastError();
+}
+
+// dst[m*N1 + n1] = W_N^((n1*m*T) mod N).
+__global__ void k_passa_twiddle(float2* dst, int N1, int R, long long T, long long N) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N1 * R) return;
+  const long long m = i / N1, n1 = i % N1;
+  dst[i] = w_of((n1 * m * T) % N, N);
+}
+
+cudaError_t passa_twiddle_fill(float2* dst, int N1, int R, long long T, long long N, cudaStream_t s) {
+  k_passa_twiddle<<<(N1 * R + 255) / 256, 256, 0, s>>>(dst, N1, R, T, N);
+  return cudaGetLastError();
+}
+
 // 4-bit complex expansion (bit-exact replacement of the reference's LUT
 // kernels complex4_expansion / copy_expand_complex4, rawspec_gpu.cu:342-374):
 // packed byte b -> real = sign-extended high nibble, imag = sign-extended low

@@ -10,7 +10,8 @@
 //           memory;
 //   pass B  N1-point FFTs along the rows k2 of that scratch, detection of
 //           the output bins X[k2 + N2*k1], integration over the unit's
-//           spectra in registers and the FFT-shifted store (or add).
+//           spectra in registers, SNORM scale and the FFT-shifted store (or
+//           add).
 //
 // X[k2 + N2 k1] = sum_n1 W_N1^(n1 k1) W_N^(n1 k2) sum_n2 x[n1 + N1 n2] W_N2^(n2 k2).
 #include <algorithm>
@@ -23,54 +24,52 @@ namespace rsg {
 
 namespace {
 
-constexpr int kLargeR = 8;
+constexpr int kRA = 16;  // radix of pass A
 constexpr int kLargeTPB = 512;
 
-template <int NSUB>
+// Sub-FFT of NSUB points at radix R; C sub-FFTs (columns or rows) per CTA,
+// interleaved across lanes so that global accesses of neighbouring lanes are
+// neighbouring columns.
+template <int NSUB, int R>
 struct LargeCfg {
-  static constexpr int R = kLargeR;
   static constexpr int T = NSUB / R;              // threads per sub-FFT
   static constexpr int C = kLargeTPB / T > 8 ? 8 : (kLargeTPB / T > 0 ? kLargeTPB / T : 1);
   static constexpr int TPB = T * C;
+  static constexpr int TW = stockham_tw_size(NSUB, R);
 };
+
+template <int POL>
+__host__ __device__ constexpr int pass_b_radix() { return POL == POL_TP ? 16 : 8; }
 
 struct BlockSyncL {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
 template <int N2, int NV>
-constexpr size_t passA_smem(int h, int logN) {
-  using Cf = LargeCfg<N2>;
-  return (size_t)N2 * sizeof(float2) + (size_t)Cf::C * NV * smem_padded_len(N2) * sizeof(float2) +
-         ((size_t)1 << h) * sizeof(float2) + ((size_t)1 << (logN - h)) * sizeof(float2);
+constexpr size_t passA_smem() {
+  using Cf = LargeCfg<N2, kRA>;
+  return (size_t)((Cf::TW + 1) & ~1) * sizeof(float2) + (size_t)Cf::C * NV * smem_padded_len(N2) * sizeof(float2);
 }
 
-template <int N1, int NV>
+template <int N1, int NV, int R>
 constexpr size_t passB_smem() {
-  using Cf = LargeCfg<N1>;
-  return (size_t)N1 * sizeof(float2) + (size_t)Cf::C * NV * smem_padded_len(N1) * sizeof(float2);
+  using Cf = LargeCfg<N1, R>;
+  return (size_t)((Cf::TW + 1) & ~1) * sizeof(float2) + (size_t)Cf::C * NV * smem_padded_len(N1) * sizeof(float2);
 }
 
 }  // namespace
 
 template <int N2, int FMT, int NV>
-__global__ void __launch_bounds__(LargeCfg<N2>::TPB)
+__global__ void __launch_bounds__(LargeCfg<N2, kRA>::TPB)
 k_large_a(LargeLaunch a) {
-  using Cf = LargeCfg<N2>;
-  constexpr int R = Cf::R, T = Cf::T, C = Cf::C, TPB = Cf::TPB;
+  using Cf = LargeCfg<N2, kRA>;
+  constexpr int R = kRA, T = Cf::T, C = Cf::C, TPB = Cf::TPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tw_s = reinterpret_cast<float2*>(smem_raw);
-  float2* xch = tw_s + N2;
-  float2* lo_s = xch + (size_t)C * NV * smem_padded_len(N2);
-  const int nlo = 1 << a.h;
-  const int nhi = 1 << (a.logN - a.h);
-  float2* hi_s = lo_s + nlo;
+  float2* xch = tw_s + ((Cf::TW + 1) & ~1);
 
   const int tid = threadIdx.x;
-  for (int i = tid; i < N2; i += TPB) tw_s[i] = a.twN2[i];
-  for (int i = tid; i < nlo; i += TPB) lo_s[i] = a.twLo[i];
-  for (int i = tid; i < nhi; i += TPB) hi_s[i] = a.twHi[i];
-  __syncthreads();
+  for (int i = tid; i < Cf::TW; i += TPB) tw_s[i] = a.twN2[i];
 
   const int N1 = 1 << a.logN1;
   const int tiles = N1 / C;
@@ -93,39 +92,43 @@ k_large_a(LargeLaunch a) {
 #pragma unroll
     for (int m = 0; m < R; ++m) {
       float2 smp[NV];
-      unpack_word(w[m], smp);
+      Unpack<FMT, NV>::run(w[m], smp);
 #pragma unroll
       for (int q = 0; q < NV; ++q) v[q][m] = smp[q];
     }
   }
+  // W_N^(n1*j) for this thread's column, from the two-level table.
+  const int e0 = n1 * j;
+  const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
+  __syncthreads();  // twiddle table in shared memory
   GroupFFT<N2, R, NV>::run(v, j, xch + (size_t)col * NV * smem_padded_len(N2), smem_padded_len(N2), tw_s,
                             BlockSyncL{});
 
-  // Twiddle W_N^(n1*k2) and store.
-  const int lomask = nlo - 1;
+  // Output k2 = j + m*T: W_N^(n1*k2) = W_N^(n1*j) * W_N^(n1*m*T).
   float2* dst = a.scratch + (size_t)slab * NV * N2 * N1 + n1;
+  const float2* twm = a.twM + n1;
 #pragma unroll
   for (int m = 0; m < R; ++m) {
     const int k2 = j + m * T;
-    const int e = n1 * k2;
-    const float2 w = cmul(lo_s[e & lomask], hi_s[e >> a.h]);
+    const float2 w = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
 #pragma unroll
     for (int q = 0; q < NV; ++q) dst[((size_t)q * N2 + k2) * N1] = cmul(v[q][m], w);
   }
 }
 
 template <int N1, int NV, int POL>
-__global__ void __launch_bounds__(LargeCfg<N1>::TPB)
+__global__ void __launch_bounds__(LargeCfg<N1, pass_b_radix<POL>()>::TPB)
 k_large_b(LargeLaunch a) {
-  using Cf = LargeCfg<N1>;
-  constexpr int R = Cf::R, T = Cf::T, C = Cf::C, TPB = Cf::TPB;
+  constexpr int R = pass_b_radix<POL>();
+  using Cf = LargeCfg<N1, R>;
+  constexpr int T = Cf::T, C = Cf::C, TPB = Cf::TPB;
   constexpr int NP = PolOut<POL>::NP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tw_s = reinterpret_cast<float2*>(smem_raw);
-  float2* xch = tw_s + N1;
+  float2* xch = tw_s + ((Cf::TW + 1) & ~1);
 
   const int tid = threadIdx.x;
-  for (int i = tid; i < N1; i += TPB) tw_s[i] = a.twN1[i];
+  for (int i = tid; i < Cf::TW; i += TPB) tw_s[i] = a.twN1[i];
   __syncthreads();
 
   const int N2 = 1 << a.logN2;
@@ -178,7 +181,7 @@ k_large_b(LargeLaunch a) {
         a.partial[(((size_t)unit * a.chunks + chunk) * NP + p) * N + f] = acc[m][p];
       } else {
         float* dst = a.out + (((size_t)d * NP + p) * a.Nc + c) * N + out_pos(f, N, a.inverse);
-        if (a.mode == ACC_ADD) *dst += acc[m][p]; else *dst = acc[m][p];
+        if (a.mode == ACC_ADD) *dst = __fmaf_rn(acc[m][p], a.scale, *dst); else *dst = acc[m][p] * a.scale;
       }
     }
   }
@@ -191,9 +194,9 @@ namespace {
 
 template <int N2, int FMT, int NV>
 cudaError_t launch_a_t(const LargeLaunch& L, cudaStream_t s, bool prep) {
-  using Cf = LargeCfg<N2>;
+  using Cf = LargeCfg<N2, kRA>;
   auto k = k_large_a<N2, FMT, NV>;
-  const size_t smem = passA_smem<N2, NV>(L.h, L.logN);
+  const size_t smem = passA_smem<N2, NV>();
   if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int N1 = 1 << L.logN1;
   const long long grid = (long long)(N1 / Cf::C) * L.Nc * L.Nss;
@@ -203,9 +206,10 @@ cudaError_t launch_a_t(const LargeLaunch& L, cudaStream_t s, bool prep) {
 
 template <int N1, int NV, int POL>
 cudaError_t launch_b_t(const LargeLaunch& L, cudaStream_t s, bool prep) {
-  using Cf = LargeCfg<N1>;
+  constexpr int R = pass_b_radix<POL>();
+  using Cf = LargeCfg<N1, R>;
   auto k = k_large_b<N1, NV, POL>;
-  const size_t smem = passB_smem<N1, NV>();
+  const size_t smem = passB_smem<N1, NV, R>();
   if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int N2 = 1 << L.logN2;
   const long long grid = (long long)(N2 / Cf::C) * L.n_units * L.chunks;
@@ -231,7 +235,6 @@ cudaError_t launch_b_n(const LargeLaunch& L, cudaStream_t s, bool prep) {
 
 cudaError_t dispatch_a(const LargeLaunch& L, cudaStream_t s, bool prep) {
   switch (L.logN2) {
-    case 6: return launch_a_n<64>(L, s, prep);
     case 7: return launch_a_n<128>(L, s, prep);
     case 8: return launch_a_n<256>(L, s, prep);
     case 9: return launch_a_n<512>(L, s, prep);
@@ -255,27 +258,37 @@ cudaError_t dispatch_b(const LargeLaunch& L, cudaStream_t s, bool prep) {
   }
 }
 
+template <int N1, int R>
+int rows_per_cta() { return LargeCfg<N1, R>::C; }
+
+int pass_b_rows(int logN1, int pol) {
+  const bool tp = pol == POL_TP;
+  switch (logN1) {
+    case 6: return tp ? rows_per_cta<64, 16>() : rows_per_cta<64, 8>();
+    case 7: return tp ? rows_per_cta<128, 16>() : rows_per_cta<128, 8>();
+    case 8: return tp ? rows_per_cta<256, 16>() : rows_per_cta<256, 8>();
+    case 9: return tp ? rows_per_cta<512, 16>() : rows_per_cta<512, 8>();
+    case 10: return tp ? rows_per_cta<1024, 16>() : rows_per_cta<1024, 8>();
+    case 11: return tp ? rows_per_cta<2048, 16>() : rows_per_cta<2048, 8>();
+    default: return tp ? rows_per_cta<4096, 16>() : rows_per_cta<4096, 8>();
+  }
+}
+
 }  // namespace
+
+int large_pass_a_radix() { return kRA; }
+int large_pass_b_radix(int pol) { return pol == POL_TP ? pass_b_radix<POL_TP>() : pass_b_radix<POL_FULL>(); }
+int stockham_table_size(int N, int R) { return stockham_tw_size(N, R); }
 
 int large_configure(LargeLaunch& L, int target_ctas, size_t* scratch_float2, size_t* partial_floats) {
   if (L.logN < 13 || L.logN > 24) return -1;
   L.logN2 = (L.logN + 1) / 2;
   L.logN1 = L.logN - L.logN2;
   L.h = (L.logN + 1) / 2;
-  const int N1 = 1 << L.logN1, N2 = 1 << L.logN2;
-  (void)N1;
+  const int N2 = 1 << L.logN2;
   const int np = L.pol == POL_TP ? 1 : 4;
   // Chunks of a unit's spectra across CTAs for parallelism.
-  int cpr;  // CTAs per unit and chunk
-  switch (L.logN1) {
-    case 6: cpr = N2 / LargeCfg<64>::C; break;
-    case 7: cpr = N2 / LargeCfg<128>::C; break;
-    case 8: cpr = N2 / LargeCfg<256>::C; break;
-    case 9: cpr = N2 / LargeCfg<512>::C; break;
-    case 10: cpr = N2 / LargeCfg<1024>::C; break;
-    case 11: cpr = N2 / LargeCfg<2048>::C; break;
-    default: cpr = N2 / LargeCfg<4096>::C; break;
-  }
+  const int cpr = N2 / pass_b_rows(L.logN1, L.pol);  // CTAs per unit and chunk
   const long long base = (long long)cpr * L.n_units;
   int chunks = (int)std::max<long long>(1, (target_ctas + base - 1) / base);
   chunks = std::min(chunks, L.M);

@@ -6,11 +6,11 @@
 // :133-267), the sub-integration `accumulate` kernel (:297-318, :1588-1601)
 // and the FFT-shifting device-to-host copies (:1647-1697):
 //
-//   int8/int16 load + SNORM conversion -> Stockham FFT in registers/shared
-//   memory (both polarisations together) -> detection -> accumulation of the
-//   unit's spectra in registers -> reduction across the CTA's thread groups
-//   -> FFT-shifted store into the dump buffer [Nd][|P|][Nc][N] (or partial
-//   sums when one unit is spread over several CTAs).
+//   int8/int16 load + exact integer unpack -> Stockham FFT in registers and
+//   shared memory (both polarisations together) -> detection -> accumulation
+//   of the unit's spectra in registers -> reduction across the CTA's thread
+//   groups -> SNORM scale and FFT-shifted store into the dump buffer
+//   [Nd][|P|][Nc][N] (or partial sums when one unit is spread over CTAs).
 //
 // Nothing but the raw voltages is read and nothing but integrated spectra is
 // written.
@@ -22,17 +22,18 @@
 
 namespace rsg {
 
-// R (values per thread per polarisation) is 8: data, twiddles and the 4*R
-// accumulators of the four-plane modes then fit the register cap of two
-// resident CTAs per SM without spilling.
+// R (values per thread per polarisation) is 16 for total power and 8 for the
+// four-plane modes, whose 4*R accumulators would otherwise not fit the
+// register cap of two resident CTAs per SM.
 template <int N, int NP>
 struct SmallCfg {
-  static constexpr int RMAX = 8;
+  static constexpr int RMAX = NP == 1 ? 16 : 8;
   static constexpr int R = N < RMAX ? N : RMAX;
   static constexpr int T = N / R;            // threads per FFT
   static constexpr int TPB = T > 256 ? T : 256;
   static constexpr int G = TPB / T;          // FFT groups per CTA
   static constexpr int MINB = 65536 / (TPB * 128) > 0 ? 65536 / (TPB * 128) : 1;
+  static constexpr int TW = stockham_tw_size(N, R);  // twiddle table entries
 };
 
 struct WarpSync {
@@ -45,7 +46,7 @@ struct BlockSync {
 template <int N, int NV, int NP>
 __host__ __device__ constexpr size_t small_smem_bytes() {
   using C = SmallCfg<N, NP>;
-  const size_t tw = (C::T > 1) ? (size_t)N * sizeof(float2) : 0;
+  const size_t tw = (size_t)((C::TW + 1) & ~1) * sizeof(float2);
   const size_t xch = (C::T > 1) ? (size_t)C::G * NV * smem_padded_len(N) * sizeof(float2) : 0;
   const size_t red = (size_t)C::TPB * C::R * NP * sizeof(float);
   return tw + (xch > red ? xch : red);
@@ -60,15 +61,15 @@ k_small(SmallLaunch a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
 
   float2* tw_s = reinterpret_cast<float2*>(smem_raw);
-  float2* xch = tw_s + ((T > 1) ? N : 0);
+  float2* xch = tw_s + ((C::TW + 1) & ~1);
   float* red = reinterpret_cast<float*>(xch);
 
   const int tid = threadIdx.x;
   const int g = tid / T;   // group within the CTA
   const int j = tid % T;   // thread within the group
 
-  if constexpr (T > 1) {
-    for (int i = tid; i < N; i += TPB) tw_s[i] = a.tw[i];
+  if constexpr (C::TW > 0) {
+    for (int i = tid; i < C::TW; i += TPB) tw_s[i] = a.tw[i];
     __syncthreads();
   }
 
@@ -111,7 +112,7 @@ k_small(SmallLaunch a) {
 #pragma unroll
       for (int m = 0; m < R; ++m) {
         float2 smp[NV];
-        unpack_word(w[m], smp);
+        Unpack<FMT, NV>::run(w[m], smp);
 #pragma unroll
         for (int q = 0; q < NV; ++q) v[q][m] = smp[q];
       }
@@ -159,12 +160,13 @@ k_small(SmallLaunch a) {
       a.partial[(((size_t)unit * a.chunks + chunk) * NP + p) * N + k] = s;
     } else {
       float* dst = a.out + (((size_t)d * NP + p) * a.Nc + c) * N + out_pos(k, N, a.inverse);
-      if (a.mode == ACC_ADD) *dst += s; else *dst = s;
+      if (a.mode == ACC_ADD) *dst = __fmaf_rn(s, a.scale, *dst); else *dst = s * a.scale;
     }
   }
 }
 
-// Finalisation of chunked units: fixed-order sum of the chunks' partials.
+// Finalisation of chunked units: fixed-order sum of the chunks' partials,
+// SNORM scale and FFT-shifted store.
 __global__ void k_finalize(FinalizeLaunch a) {
   const long long total = (long long)a.n_units * a.np * a.N;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
@@ -179,7 +181,7 @@ __global__ void k_finalize(FinalizeLaunch a) {
     const int c = unit / a.units_per_chan;
     const int d = unit % a.units_per_chan;
     float* dst = a.out + (((size_t)d * a.np + p) * a.Nc + c) * a.N + out_pos(k, a.N, a.inverse);
-    if (a.mode == ACC_ADD) *dst += s; else *dst = s;
+    if (a.mode == ACC_ADD) *dst = __fmaf_rn(s, a.scale, *dst); else *dst = s * a.scale;
   }
 }
 
@@ -249,6 +251,8 @@ cudaError_t launch_fmt(const SmallLaunch& L, cudaStream_t s, bool prep) {
 }
 
 }  // namespace
+
+int small_radix(int logN, int pol) { return small_info_dyn(logN, 2, pol).R; }
 
 int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats) {
   if (L.logN < 0 || L.logN > 12 || L.M < 1 || L.n_units < 1) return -1;

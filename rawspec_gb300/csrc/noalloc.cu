@@ -98,6 +98,8 @@ extern "C" int rawspec_gb300_product_noalloc(const void* d_in, unsigned int Nc, 
   L.mode = ACC_WRITE;
   L.inverse = fft_dir <= 0 ? 1 : 0;
   L.conj = input_conjugated ? 1 : 0;
+  const float snorm_d = Nbps == 16 ? 32767.0f : 127.0f;
+  L.scale = 1.0f / (snorm_d * snorm_d);
 
   int sms = 152;
   int dev = 0;
@@ -116,7 +118,7 @@ extern "C" int rawspec_gb300_product_noalloc(const void* d_in, unsigned int Nc, 
     fprintf(stderr, "rawspec_gb300_product_noalloc: partial sums exceed the %zu-float scratch\n", kPartialFloats);
     return 1;
   }
-  cudaError_t e = twiddle_fill(tw, (long long)Nt, (long long)Nt, 1, s);
+  cudaError_t e = stockham_twiddle_fill(tw, (int)Nt, small_radix(L.logN, L.pol), s);
   if (e == cudaSuccess) e = small_prepare(L);
   if (e == cudaSuccess) e = small_launch(L, s);
   if (e == cudaSuccess && L.chunks > 1) {
@@ -131,6 +133,7 @@ extern "C" int rawspec_gb300_product_noalloc(const void* d_in, unsigned int Nc, 
     F.units_per_chan = L.units_per_chan;
     F.mode = ACC_WRITE;
     F.inverse = L.inverse;
+    F.scale = L.scale;
     e = finalize_launch(F, s);
   }
   if (e != cudaSuccess) {

@@ -58,7 +58,7 @@ struct Product {
   size_t out_bytes = 0;
   float* d_ics = nullptr;
   size_t ics_bytes = 0;
-  float2* d_tw = nullptr;  // small: W_N; large: W_N2 | W_N1 | lo | hi
+  float2* d_tw = nullptr;  // small: Stockham table; large: A table | B table | lo | hi | pass-A output twiddles
   SmallLaunch sl;
   LargeLaunch ll;
   int chunks = 1;
@@ -353,6 +353,26 @@ int dev_alloc(GpuCtx* g, T** p, size_t bytes) {
   return 0;
 }
 
+int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int n_units, int chunks, int upc, int mode,
+                    int inverse, float scale) {
+  FinalizeLaunch F;
+  F.partial = g->d_partial;
+  F.out = P.d_out;
+  F.n_units = n_units;
+  F.chunks = chunks;
+  F.np = P.np;
+  F.N = P.N;
+  F.Nc = (int)ctx->Nc;
+  F.units_per_chan = upc;
+  F.mode = mode;
+  F.inverse = inverse;
+  F.scale = scale;
+  ProfScope ps(g, RAWSPEC_GB300_K_FINALIZE);
+  RSG_CUDA(finalize_launch(F, g->stream));
+  g->launches++;
+  return 0;
+}
+
 int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse) {
   Product& P = g->prod[i];
   if (!P.large) {
@@ -364,22 +384,8 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
       RSG_CUDA(small_launch(L, g->stream));
       g->launches++;
     }
-    if (L.chunks > 1) {
-      FinalizeLaunch F;
-      F.partial = g->d_partial;
-      F.out = P.d_out;
-      F.n_units = L.n_units;
-      F.chunks = L.chunks;
-      F.np = P.np;
-      F.N = P.N;
-      F.Nc = (int)ctx->Nc;
-      F.units_per_chan = L.units_per_chan;
-      F.mode = mode;
-      F.inverse = inverse;
-      ProfScope ps(g, RAWSPEC_GB300_K_FINALIZE);
-      RSG_CUDA(finalize_launch(F, g->stream));
-      g->launches++;
-    }
+    if (L.chunks > 1 && launch_finalize(ctx, g, P, L.n_units, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+      return 1;
   } else {
     LargeLaunch L = P.ll;
     L.mode = mode;
@@ -394,22 +400,8 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
       RSG_CUDA(large_launch_b(L, g->stream));
       g->launches++;
     }
-    if (L.chunks > 1) {
-      FinalizeLaunch F;
-      F.partial = g->d_partial;
-      F.out = P.d_out;
-      F.n_units = L.n_units;
-      F.chunks = L.chunks;
-      F.np = P.np;
-      F.N = P.N;
-      F.Nc = (int)ctx->Nc;
-      F.units_per_chan = L.units_per_chan;
-      F.mode = mode;
-      F.inverse = inverse;
-      ProfScope ps(g, RAWSPEC_GB300_K_FINALIZE);
-      RSG_CUDA(finalize_launch(F, g->stream));
-      g->launches++;
-    }
+    if (L.chunks > 1 && launch_finalize(ctx, g, P, L.n_units, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+      return 1;
   }
   return 0;
 }
@@ -526,7 +518,10 @@ int rawspec_initialize(rawspec_context* ctx) {
     CK(cudaMemcpy(g->d_aws, w.data(), ctx->Nant * sizeof(float), cudaMemcpyHostToDevice));
   }
 
-  // Products.
+  // Products.  The kernels work on the integer codes; the SNORM scale
+  // (1/127 or 1/32767 per component) is applied to the quadratic products.
+  const float snorm_d = ctx->Nbps == 16 ? 32767.0f : 127.0f;
+  const float scale = 1.0f / (snorm_d * snorm_d);
   const int target_ctas = g->sm_count * 4;
   size_t partial_need = 0, scratch_need = 0;
   for (unsigned i = 0; i < ctx->No; i++) {
@@ -572,9 +567,12 @@ int rawspec_initialize(rawspec_context* ctx) {
         FAIL();
       }
       partial_need = std::max(partial_need, pf);
-      if (dev_alloc(g, &P.d_tw, (size_t)P.N * sizeof(float2))) FAIL();
-      CK(twiddle_fill(P.d_tw, P.N, P.N, 1, g->stream));
+      const int R = small_radix(P.logN, pol);
+      const size_t ntw = (size_t)std::max(stockham_table_size(P.N, R), 1);
+      if (dev_alloc(g, &P.d_tw, ntw * sizeof(float2))) FAIL();
+      CK(stockham_twiddle_fill(P.d_tw, P.N, R, g->stream));
       L.tw = P.d_tw;
+      L.scale = scale;
       CK(small_prepare(L));
     } else {
       LargeLaunch& L = P.ll;
@@ -598,17 +596,22 @@ int rawspec_initialize(rawspec_context* ctx) {
       }
       scratch_need = std::max(scratch_need, sf);
       partial_need = std::max(partial_need, pf);
-      const size_t n1 = (size_t)1 << L.logN1, n2 = (size_t)1 << L.logN2;
-      const size_t nlo = (size_t)1 << L.h, nhi = (size_t)1 << (L.logN - L.h);
-      if (dev_alloc(g, &P.d_tw, (n1 + n2 + nlo + nhi) * sizeof(float2))) FAIL();
+      const int n1 = 1 << L.logN1, n2 = 1 << L.logN2;
+      const int RA = large_pass_a_radix(), RB = large_pass_b_radix(pol);
+      const size_t ta = (size_t)stockham_table_size(n2, RA), tb = (size_t)stockham_table_size(n1, RB);
+      const size_t nlo = (size_t)1 << L.h, nhi = (size_t)1 << (L.logN - L.h), nm = (size_t)RA * n1;
+      if (dev_alloc(g, &P.d_tw, (ta + tb + nlo + nhi + nm) * sizeof(float2))) FAIL();
       L.twN2 = P.d_tw;
-      L.twN1 = P.d_tw + n2;
-      L.twLo = P.d_tw + n2 + n1;
-      L.twHi = P.d_tw + n2 + n1 + nlo;
-      CK(twiddle_fill(P.d_tw, (long long)n2, (long long)n2, 1, g->stream));
-      CK(twiddle_fill(P.d_tw + n2, (long long)n1, (long long)n1, 1, g->stream));
-      CK(twiddle_fill(P.d_tw + n2 + n1, (long long)nlo, (long long)P.N, 1, g->stream));
-      CK(twiddle_fill(P.d_tw + n2 + n1 + nlo, (long long)nhi, (long long)P.N, (long long)nlo, g->stream));
+      L.twN1 = P.d_tw + ta;
+      L.twLo = P.d_tw + ta + tb;
+      L.twHi = P.d_tw + ta + tb + nlo;
+      L.twM = P.d_tw + ta + tb + nlo + nhi;
+      L.scale = scale;
+      CK(stockham_twiddle_fill(P.d_tw, n2, RA, g->stream));
+      CK(stockham_twiddle_fill(P.d_tw + ta, n1, RB, g->stream));
+      CK(twiddle_fill(P.d_tw + ta + tb, (long long)nlo, (long long)P.N, 1, g->stream));
+      CK(twiddle_fill(P.d_tw + ta + tb + nlo, (long long)nhi, (long long)P.N, (long long)nlo, g->stream));
+      CK(passa_twiddle_fill(P.d_tw + ta + tb + nlo + nhi, n1, RA, (long long)(n2 / RA), (long long)P.N, g->stream));
       CK(large_prepare(L));
     }
   }
