@@ -25,7 +25,8 @@ namespace rsg {
 namespace {
 
 constexpr int kRA = 16;  // radix of pass A
-constexpr int kLargeTPB = 512;
+constexpr int kLargeTPB = 256;
+constexpr int kLargeMinBlocks = 2;  // resident CTAs per SM the register budget allows
 
 // Sub-FFT of NSUB points at radix R; C sub-FFTs (columns or rows) per CTA,
 // interleaved across lanes so that global accesses of neighbouring lanes are
@@ -60,7 +61,7 @@ constexpr size_t passB_smem() {
 }  // namespace
 
 template <int N2, int FMT, int NV>
-__global__ void __launch_bounds__(LargeCfg<N2, kRA>::TPB)
+__global__ void __launch_bounds__(LargeCfg<N2, kRA>::TPB, kLargeMinBlocks)
 k_large_a(LargeLaunch a) {
   using Cf = LargeCfg<N2, kRA>;
   constexpr int R = kRA, T = Cf::T, C = Cf::C, TPB = Cf::TPB;
@@ -117,7 +118,7 @@ k_large_a(LargeLaunch a) {
 }
 
 template <int N1, int NV, int POL>
-__global__ void __launch_bounds__(LargeCfg<N1, pass_b_radix<POL>()>::TPB)
+__global__ void __launch_bounds__(LargeCfg<N1, pass_b_radix<POL>()>::TPB, kLargeMinBlocks)
 k_large_b(LargeLaunch a) {
   constexpr int R = pass_b_radix<POL>();
   using Cf = LargeCfg<N1, R>;
