@@ -91,6 +91,11 @@ struct LargeLaunch {
   int h = 0;
   int mode = ACC_WRITE, inverse = 0, conj = 0;
   float scale = 1.0f;
+  // persistent fused kernel (one spectrum per integration unit)
+  int S = 0;                      // slabs per buffer (Nc * Nss)
+  int ring = 0;                   // intermediate slots
+  int* ctl = nullptr;             // [0] error, [1] item counter, [2..2+S) A done, [2+S..2+2S) B done
+  int fused_ctas = 0;             // persistent grid size
 };
 int large_configure(LargeLaunch& L, int target_ctas, size_t* scratch_float2, size_t* partial_floats);
 // Radix of pass A (values per thread of its N2-point FFT) and its threads per
@@ -104,6 +109,15 @@ cudaError_t large_launch_a(const LargeLaunch& L, cudaStream_t s);
 cudaError_t large_launch_b(const LargeLaunch& L, cudaStream_t s);
 // Raises both kernels' dynamic shared-memory limits on the current device.
 cudaError_t large_prepare(const LargeLaunch& L);
+// Persistent fused variant (k_large_fused.cu): supported for 8-bit input,
+// 2^16 <= N <= 2^22 and integration units of one spectrum; needs a ring of
+// large_fused_ring() intermediate slabs and large_fused_ctl_ints() control
+// words (zeroed once before the first launch).
+bool large_fused_supported(const LargeLaunch& L);
+int large_fused_ring();
+int large_fused_ctl_ints(const LargeLaunch& L);
+cudaError_t large_fused_prepare(LargeLaunch& L);
+cudaError_t large_fused_launch(const LargeLaunch& L, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Auxiliary kernels.

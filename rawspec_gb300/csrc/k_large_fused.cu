@@ -1,0 +1,301 @@
+// k_large_fused.cu -- persistent four-step FFT spectrometer for long
+// transforms whose integration unit is one spectrum per buffer (the case of
+// the 2^20-point product of the production configuration).
+//
+// The two passes of the four-step FFT (see k_large.cu) become work items of
+// one persistent kernel, taken in a fixed order through an atomic counter:
+//
+//   A(0) A(1) B(0) A(2) B(1) ... A(S-1) B(S-2) B(S-1)
+//
+// where A(s) are the column tiles of slab s (one channel-spectrum, both
+// polarisations) and B(s) its row tiles.  A(s) writes the FP32 intermediate
+// into slot s mod RING of a small ring (RING slabs, sized to stay in L2);
+// B(s) waits until every A(s) tile is published, A(s) waits until every
+// B(s-RING) tile has released the slot.  An item only ever waits for items
+// earlier in the order, which were taken by CTAs that are running, so the
+// waits always end; they are bounded nonetheless and record an error instead
+// of hanging if the bound is ever reached.  Column and row tiles of
+// neighbouring slabs run side by side on the SMs, so the loads of one overlap
+// the arithmetic of another, and the intermediate rarely leaves L2.
+#include <algorithm>
+
+#include "detect.cuh"
+#include "fft_core.cuh"
+#include "internal.h"
+
+namespace rsg {
+
+namespace {
+
+constexpr int kFusedTPB = 256;
+constexpr int kFusedMinBlocks = 2;
+constexpr int kRingSlots = 4;
+constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
+
+template <int POL>
+__host__ __device__ constexpr int fused_rb() { return POL == POL_TP ? 16 : 8; }
+
+// Shared-memory distance between the exchange buffers of neighbouring
+// interleaved sub-FFTs, chosen so that the C sub-FFTs served by one
+// half-warp land on disjoint banks.
+__host__ __device__ constexpr int group_stride(int N, int NV, int C) {
+  int base = NV * smem_padded_len(N);
+  const int cp = C < 16 ? C : 16;
+  const int want = (16 / cp) % 16;
+  while (base % 16 != want) ++base;
+  return base;
+}
+
+template <int N1, int N2, int NV, int POL>
+struct FusedCfg {
+  static constexpr int RA = 16, TA = N2 / RA, CA = kFusedTPB / TA;
+  static constexpr int RB = fused_rb<POL>(), TB = N1 / RB, CB = kFusedTPB / TB;
+  static constexpr int TWA = stockham_tw_size(N2, RA), TWB = stockham_tw_size(N1, RB);
+  static constexpr int TWA2 = (TWA + 1) & ~1, TWB2 = (TWB + 1) & ~1;
+  static constexpr int GSA = group_stride(N2, NV, CA), GSB = group_stride(N1, NV, CB);
+  static constexpr int XCH = CA * GSA > CB * GSB ? CA * GSA : CB * GSB;
+  static constexpr size_t SMEM = (size_t)(TWA2 + TWB2 + XCH) * sizeof(float2);
+  static_assert(TA * CA == kFusedTPB && TB * CB == kFusedTPB, "sub-FFT threads must tile the CTA");
+};
+
+struct Sync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
+__device__ __forceinline__ int load_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Thread 0 polls until *cnt reaches target (bounded; on time-out it records
+// `code` in the error word and lets the CTA proceed), then the CTA proceeds.
+__device__ __forceinline__ void wait_count(const int* cnt, int target, int* err, int code) {
+  if (threadIdx.x == 0) {
+    unsigned ns = 32;
+    long long it = 0;
+    while (load_acquire(cnt) < target) {
+      if (++it > kSpinLimit) {
+        atomicExch(err, code);
+        break;
+      }
+      __nanosleep(ns);
+      if (ns < 256) ns *= 2;
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+// All threads' global writes of the tile become visible, then the tile is
+// counted.
+__device__ __forceinline__ void publish(int* cnt) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(cnt, 1);
+}
+
+}  // namespace
+
+template <int N1, int N2, int FMT, int NV, int POL>
+__global__ void __launch_bounds__(kFusedTPB, kFusedMinBlocks)
+k_large_fused(LargeLaunch a) {
+  using F = FusedCfg<N1, N2, NV, POL>;
+  constexpr int N = N1 * N2;
+  constexpr int NP = PolOut<POL>::NP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* twA = reinterpret_cast<float2*>(smem_raw);
+  float2* twB = twA + F::TWA2;
+  float2* xch = twB + F::TWB2;
+  __shared__ long long s_item;
+
+  const int tid = threadIdx.x;
+  for (int i = tid; i < F::TWA; i += kFusedTPB) twA[i] = a.twN2[i];
+  for (int i = tid; i < F::TWB; i += kFusedTPB) twB[i] = a.twN1[i];
+  __syncthreads();
+
+  const int S = a.S;
+  constexpr int tilesA = N1 / F::CA, tilesB = N2 / F::CB;
+  const long long total = (long long)S * (tilesA + tilesB);
+  int* err = a.ctl;       // sticky error word (never reset by a launch)
+  int* next = a.ctl + 1;
+  int* doneA = a.ctl + 2;
+  int* doneB = a.ctl + 2 + S;
+  const float im_sign = a.conj ? -1.0f : 1.0f;
+
+  for (;;) {
+    if (tid == 0) s_item = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= total) break;
+
+    // Decode the item: A(0) | [A(k) B(k-1)] for k = 1..S-1 | B(S-1).
+    bool isA;
+    int slab, tile;
+    if (item < tilesA) {
+      isA = true;
+      slab = 0;
+      tile = (int)item;
+    } else {
+      const long long j = item - tilesA;
+      const int k = (int)(j / (tilesA + tilesB)) + 1;
+      const int r = (int)(j % (tilesA + tilesB));
+      if (k <= S - 1 && r < tilesA) {
+        isA = true;
+        slab = k;
+        tile = r;
+      } else {
+        isA = false;
+        slab = k - 1;
+        tile = k <= S - 1 ? r - tilesA : r;
+      }
+    }
+    const int slot = slab % a.ring;
+    float2* scr = a.scratch + (size_t)slot * NV * N;
+
+    if (isA) {
+      if (slab >= a.ring) wait_count(doneB + (slab - a.ring), tilesB, err, 1);
+      // ---- column tile: N2-point FFTs of C_A columns n1 --------------------
+      constexpr int R = F::RA, T = F::TA, C = F::CA;
+      const int col = tid % C;
+      const int j = tid / C;
+      const int n1 = tile * C + col;
+      const int c = slab / a.Nss;
+      const int sp = slab % a.Nss;
+      using W = typename SampleWord<FMT, NV>::type;
+      const W* src = reinterpret_cast<const W*>(a.in) + (long long)c * a.chan_stride + (long long)sp * N + n1 +
+                     (long long)N1 * j;
+      float2 v[NV][R];
+      {
+        W w[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) w[m] = __ldg(src + (long long)N1 * T * m);
+#pragma unroll
+        for (int m = 0; m < R; ++m) {
+          float2 smp[NV];
+          Unpack<FMT, NV>::run(w[m], smp);
+#pragma unroll
+          for (int q = 0; q < NV; ++q) v[q][m] = smp[q];
+        }
+      }
+      const int e0 = n1 * j;
+      const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
+      GroupFFT<N2, R, NV>::run(v, j, xch + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
+      float2* dst = scr + n1;
+      const float2* twm = a.twM + n1;
+#pragma unroll
+      for (int m = 0; m < R; ++m) {
+        const int k2 = j + m * T;
+        const float2 w = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
+#pragma unroll
+        for (int q = 0; q < NV; ++q) __stcg(dst + ((size_t)q * N2 + k2) * N1, cmul(v[q][m], w));
+      }
+      publish(doneA + slab);
+    } else {
+      wait_count(doneA + slab, tilesA, err, 2);
+      // ---- row tile: N1-point FFTs of C_B rows k2, detection, store -------
+      constexpr int R = F::RB, T = F::TB, C = F::CB;
+      const int row = tid % C;
+      const int j = tid / C;
+      const int k2 = tile * C + row;
+      const int c = slab / a.units_per_chan;
+      const int d = slab % a.units_per_chan;
+      const float2* src = scr + (size_t)k2 * N1 + j;
+      float2 v[NV][R];
+#pragma unroll
+      for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int m = 0; m < R; ++m) v[q][m] = __ldcg(src + (size_t)q * N2 * N1 + m * T);
+      GroupFFT<N1, R, NV>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
+#pragma unroll
+      for (int m = 0; m < R; ++m) {
+        float2 x[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = v[q][m];
+        float acc[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
+        detect_acc<POL, NV>(acc, x, im_sign);
+        const int f = k2 + N2 * (j + m * T);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          float* o = a.out + (((size_t)d * NP + p) * a.Nc + c) * N + out_pos(f, N, a.inverse);
+          if (a.mode == ACC_ADD) *o = __fmaf_rn(acc[p], a.scale, *o); else *o = acc[p] * a.scale;
+        }
+      }
+      publish(doneB + slab);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+namespace {
+
+template <int N1, int N2, int NV, int POL>
+cudaError_t fused_t(const LargeLaunch& L, cudaStream_t s, int mode_op, int* ctas_out) {
+  using F = FusedCfg<N1, N2, NV, POL>;
+  auto k = k_large_fused<N1, N2, FMT_I8, NV, POL>;
+  if (mode_op == 1) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F::SMEM);
+  if (mode_op == 2) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kFusedTPB, F::SMEM);
+    if (e != cudaSuccess) return e;
+    *ctas_out = std::max(1, per_sm) * sms;
+    return cudaSuccess;
+  }
+  k<<<L.fused_ctas, kFusedTPB, F::SMEM, s>>>(L);
+  return cudaGetLastError();
+}
+
+template <int N1, int N2>
+cudaError_t fused_pol(const LargeLaunch& L, cudaStream_t s, int op, int* ctas) {
+  if (L.nv == 1) return fused_t<N1, N2, 1, POL_TP>(L, s, op, ctas);
+  switch (L.pol) {
+    case POL_FULL: return fused_t<N1, N2, 2, POL_FULL>(L, s, op, ctas);
+    case POL_STOKES: return fused_t<N1, N2, 2, POL_STOKES>(L, s, op, ctas);
+    default: return fused_t<N1, N2, 2, POL_TP>(L, s, op, ctas);
+  }
+}
+
+cudaError_t fused_dispatch(const LargeLaunch& L, cudaStream_t s, int op, int* ctas) {
+  switch (L.logN) {
+    case 16: return fused_pol<256, 256>(L, s, op, ctas);
+    case 17: return fused_pol<256, 512>(L, s, op, ctas);
+    case 18: return fused_pol<512, 512>(L, s, op, ctas);
+    case 19: return fused_pol<512, 1024>(L, s, op, ctas);
+    case 20: return fused_pol<1024, 1024>(L, s, op, ctas);
+    case 21: return fused_pol<1024, 2048>(L, s, op, ctas);
+    case 22: return fused_pol<2048, 2048>(L, s, op, ctas);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+bool large_fused_supported(const LargeLaunch& L) {
+  return L.fmt == FMT_I8 && L.M == 1 && L.logN >= 16 && L.logN <= 22 && L.logN2 == (L.logN + 1) / 2;
+}
+
+int large_fused_ring() { return kRingSlots; }
+
+int large_fused_ctl_ints(const LargeLaunch& L) { return 2 + 2 * L.Nc * L.Nss; }
+
+cudaError_t large_fused_prepare(LargeLaunch& L) {
+  cudaError_t e = fused_dispatch(L, nullptr, 1, nullptr);
+  if (e != cudaSuccess) return e;
+  return fused_dispatch(L, nullptr, 2, &L.fused_ctas);
+}
+
+cudaError_t large_fused_launch(const LargeLaunch& L, cudaStream_t s) {
+  // reset the item counter and the per-slab counters; ctl[0] keeps errors
+  cudaError_t e = cudaMemsetAsync(L.ctl + 1, 0, sizeof(int) * (size_t)(large_fused_ctl_ints(L) - 1), s);
+  if (e != cudaSuccess) return e;
+  return fused_dispatch(L, s, 0, nullptr);
+}
+
+}  // namespace rsg

@@ -62,6 +62,8 @@ struct Product {
   SmallLaunch sl;
   LargeLaunch ll;
   int chunks = 1;
+  bool fused = false;      // persistent fused four-step kernel
+  int* d_ctl = nullptr;    // its control words
 };
 
 struct DumpCb {
@@ -390,6 +392,12 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
     LargeLaunch L = P.ll;
     L.mode = mode;
     L.inverse = inverse;
+    if (P.fused) {
+      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_FUSED);
+      RSG_CUDA(large_fused_launch(L, g->stream));
+      g->launches++;
+      return 0;
+    }
     {
       ProfScope ps(g, RAWSPEC_GB300_K_LARGE_A);
       RSG_CUDA(large_launch_a(L, g->stream));
@@ -594,6 +602,17 @@ int rawspec_initialize(rawspec_context* ctx) {
         fprintf(stderr, "unsupported FFT length %d\n", P.N);
         FAIL();
       }
+      if (large_fused_supported(L)) {
+        P.fused = true;
+        L.S = (int)ctx->Nc * (int)P.Nss;
+        L.ring = large_fused_ring();
+        sf = (size_t)L.ring * L.nv * ((size_t)1 << L.logN);
+        pf = 0;
+        const size_t nctl = (size_t)large_fused_ctl_ints(L);
+        if (dev_alloc(g, &P.d_ctl, nctl * sizeof(int))) FAIL();
+        CK(cudaMemsetAsync(P.d_ctl, 0, nctl * sizeof(int), g->stream));
+        L.ctl = P.d_ctl;
+      }
       scratch_need = std::max(scratch_need, sf);
       partial_need = std::max(partial_need, pf);
       const int n1 = 1 << L.logN1, n2 = 1 << L.logN2;
@@ -612,7 +631,8 @@ int rawspec_initialize(rawspec_context* ctx) {
       CK(twiddle_fill(P.d_tw + ta + tb, (long long)nlo, (long long)P.N, 1, g->stream));
       CK(twiddle_fill(P.d_tw + ta + tb + nlo, (long long)nhi, (long long)P.N, (long long)nlo, g->stream));
       CK(passa_twiddle_fill(P.d_tw + ta + tb + nlo + nhi, n1, RA, (long long)(n2 / RA), (long long)P.N, g->stream));
-      CK(large_prepare(L));
+      if (P.fused) CK(large_fused_prepare(L));
+      else CK(large_prepare(L));
     }
   }
   if (partial_need) {
@@ -666,6 +686,7 @@ void rawspec_cleanup(rawspec_context* ctx) {
     cudaFree(g->prod[i].d_out);
     cudaFree(g->prod[i].d_ics);
     cudaFree(g->prod[i].d_tw);
+    cudaFree(g->prod[i].d_ctl);
   }
   for (auto& p : g->pending) {
     cudaEventDestroy(p.a);
@@ -815,6 +836,15 @@ int rawspec_wait_for_completion(rawspec_context* ctx) {
   if (!g) return 1;
   for (unsigned i = 0; i < ctx->No; i++) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) return 1;
+  for (unsigned i = 0; i < ctx->No; i++) {
+    if (!g->prod[i].d_ctl) continue;
+    int err = 0;
+    if (cudaMemcpy(&err, g->prod[i].d_ctl, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    if (err) {
+      fprintf(stderr, "rawspec: product %u: a dependency wait of the fused FFT kernel timed out (code %d)\n", i, err);
+      return 1;
+    }
+  }
   if (ctx->exit_soon)
     fprintf(stderr, "*** rawspec_wait_for_completion detected exit_soon enabled.\n*** Cannot continue!\n");
   return (int)ctx->exit_soon;

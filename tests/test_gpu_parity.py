@@ -81,6 +81,20 @@ def test_large_lengths(cuda_device, logn):
     assert err < REL_TOL, (nt, err)
 
 
+@pytest.mark.parametrize("npol,conj,fft_dir", [(1, 0, 1), (4, 1, -1), (-4, 1, 1)])
+def test_fused_long_fft_many_slabs(cuda_device, npol, conj, fft_dir):
+    # 2^16-point FFTs, one spectrum per integration, 4 spectra per channel
+    # and 3 channels: 12 slabs pass through the 4-slot intermediate ring of
+    # the persistent kernel, so slot reuse and both dependency waits occur.
+    nt, Ntpb = 1 << 16, 1 << 18
+    c = dict(Nc=3, Np=2, Ntpb=Ntpb, nbits=8, nblocks=1, products=[(nt, 1, npol)], conj=conj, fft_dir=fft_dir)
+    blocks = synth.gaussian_blocks(1, 3, Ntpb, 2, sigma=20.0, seed=300 + npol)
+    dumps, _, _, _ = run_gpu(c, blocks)
+    ref, _ = oracle_for(c, blocks)
+    assert dumps[0].shape == ref[0].shape
+    assert normalized_error(dumps[0], ref[0], npol, 3, nt) < REL_TOL
+
+
 def test_inverse_direction_and_nis_chunks(cuda_device):
     c = dict(Nc=4, Np=2, Ntpb=8192, nbits=8, nblocks=6, products=[(1024, 24, -4), (8192, 3, 1)], conj=1, fft_dir=-1)
     blocks = synth.gaussian_blocks(6, 4, 8192, 2, sigma=20.0, seed=7)
