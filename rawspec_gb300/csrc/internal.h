@@ -45,6 +45,7 @@ struct SmallLaunch {
   // per call
   int mode = ACC_WRITE, inverse = 0, conj = 0;
   float scale = 1.0f;         // SNORM scale squared, applied to the results
+  int vec16 = 0;              // spectra start on 16-byte boundaries (set by small_configure)
 };
 
 // Chooses block size, units per block and chunks per unit.  target_ctas is

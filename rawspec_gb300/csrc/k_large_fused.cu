@@ -32,8 +32,10 @@ constexpr int kFusedMinBlocks = 2;
 constexpr int kRingSlots = 4;
 constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
 
+// Row tiles hold no multi-spectrum accumulators (one spectrum per unit), so
+// all modes run at radix 16.
 template <int POL>
-__host__ __device__ constexpr int fused_rb() { return POL == POL_TP ? 16 : 8; }
+__host__ __device__ constexpr int fused_rb() { return 16; }
 
 // Shared-memory distance between the exchange buffers of neighbouring
 // interleaved sub-FFTs, chosen so that the C sub-FFTs served by one
@@ -88,12 +90,67 @@ __device__ __forceinline__ void wait_count(const int* cnt, int target, int* err,
 }
 
 // All threads' global writes of the tile become visible, then the tile is
-// counted.
+// counted: the CTA barrier orders every thread's writes before thread 0's
+// device-scope fence and release of the counter (the same pattern as a grid
+// barrier).
 __device__ __forceinline__ void publish(int* cnt) {
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) atomicAdd(cnt, 1);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(cnt, 1);
+  }
 }
+
+// L2 eviction-priority policies: streams read or written once are marked
+// evict-first, the ring intermediate (re-read soon) evict-last.
+__device__ __forceinline__ unsigned long long policy_evict_first() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ unsigned long long policy_evict_last() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint32_t ld_u32_hint(const uint32_t* p, unsigned long long pol) {
+  uint32_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint16_t ld_u16_hint(const uint16_t* p, unsigned long long pol) {
+  uint16_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_f2_hint(float2* p, float2 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ float2 ld_f2_hint(const float2* p, unsigned long long pol) {
+  float2 v;
+  asm volatile("ld.global.cg.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol)
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ float ld_f_hint(const float* p, unsigned long long pol) {
+  float v;
+  asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_f_hint(float* p, float v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
+}
+template <typename W>
+struct HintLoad;
+template <>
+struct HintLoad<uint32_t> {
+  static __device__ __forceinline__ uint32_t ld(const uint32_t* p, unsigned long long pol) { return ld_u32_hint(p, pol); }
+};
+template <>
+struct HintLoad<uint16_t> {
+  static __device__ __forceinline__ uint16_t ld(const uint16_t* p, unsigned long long pol) { return ld_u16_hint(p, pol); }
+};
 
 }  // namespace
 
@@ -122,6 +179,8 @@ k_large_fused(LargeLaunch a) {
   int* doneA = a.ctl + 2;
   int* doneB = a.ctl + 2 + S;
   const float im_sign = a.conj ? -1.0f : 1.0f;
+  const unsigned long long pol_first = policy_evict_first();
+  const unsigned long long pol_last = policy_evict_last();
 
   for (;;) {
     if (tid == 0) s_item = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
@@ -170,7 +229,7 @@ k_large_fused(LargeLaunch a) {
       {
         W w[R];
 #pragma unroll
-        for (int m = 0; m < R; ++m) w[m] = __ldg(src + (long long)N1 * T * m);
+        for (int m = 0; m < R; ++m) w[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
 #pragma unroll
         for (int m = 0; m < R; ++m) {
           float2 smp[NV];
@@ -189,7 +248,7 @@ k_large_fused(LargeLaunch a) {
         const int k2 = j + m * T;
         const float2 w = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
 #pragma unroll
-        for (int q = 0; q < NV; ++q) __stcg(dst + ((size_t)q * N2 + k2) * N1, cmul(v[q][m], w));
+        for (int q = 0; q < NV; ++q) st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[q][m], w), pol_last);
       }
       publish(doneA + slab);
     } else {
@@ -206,7 +265,7 @@ k_large_fused(LargeLaunch a) {
 #pragma unroll
       for (int q = 0; q < NV; ++q)
 #pragma unroll
-        for (int m = 0; m < R; ++m) v[q][m] = __ldcg(src + (size_t)q * N2 * N1 + m * T);
+        for (int m = 0; m < R; ++m) v[q][m] = ld_f2_hint(src + (size_t)q * N2 * N1 + m * T, pol_first);
       GroupFFT<N1, R, NV>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
 #pragma unroll
       for (int m = 0; m < R; ++m) {
@@ -221,7 +280,8 @@ k_large_fused(LargeLaunch a) {
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
           float* o = a.out + (((size_t)d * NP + p) * a.Nc + c) * N + out_pos(f, N, a.inverse);
-          if (a.mode == ACC_ADD) *o = __fmaf_rn(acc[p], a.scale, *o); else *o = acc[p] * a.scale;
+          const float val = a.mode == ACC_ADD ? __fmaf_rn(acc[p], a.scale, ld_f_hint(o, pol_first)) : acc[p] * a.scale;
+          st_f_hint(o, val, pol_first);
         }
       }
       publish(doneB + slab);

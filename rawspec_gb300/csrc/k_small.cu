@@ -39,8 +39,14 @@ struct SmallCfg {
 struct WarpSync {
   __device__ __forceinline__ void operator()() const { __syncwarp(); }
 };
-struct BlockSync {
-  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+// Barrier of one transform group that spans whole warps (named barrier
+// 1 + group, `threads` = the group's thread count), so that the groups of a
+// CTA progress independently.
+struct GroupSync {
+  int id, threads;
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+  }
 };
 
 template <int N, int NV, int NP>
@@ -107,8 +113,19 @@ k_small(SmallLaunch a) {
       using W = typename SampleWord<FMT, NV>::type;
       const W* src = reinterpret_cast<const W*>(a.in) + chan_base + (unit_first_spec + s_local) * N + j;
       W w[R];
+      constexpr bool kVec = T == 1 && (R * sizeof(W)) % 16 == 0;
+      if (kVec && a.vec16) {
+        // one thread per transform: its R contiguous words in 16-byte loads
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
 #pragma unroll
-      for (int m = 0; m < R; ++m) w[m] = __ldg(src + m * T);
+        for (int i = 0; i < (int)(R * sizeof(W) / 16); ++i) {
+          const uint4 u = __ldg(s4 + i);
+          memcpy(reinterpret_cast<char*>(w) + 16 * i, &u, 16);
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < R; ++m) w[m] = __ldg(src + m * T);
+      }
 #pragma unroll
       for (int m = 0; m < R; ++m) {
         float2 smp[NV];
@@ -123,7 +140,8 @@ k_small(SmallLaunch a) {
         for (int q = 0; q < NV; ++q) v[q][m] = make_float2(0.f, 0.f);
     }
     if constexpr (T > 32) {
-      GroupFFT<N, R, NV>::run(v, j, my_xch, smem_padded_len(N), tw_s, BlockSync{});
+      static_assert(G <= 15, "one named barrier per group");
+      GroupFFT<N, R, NV>::run(v, j, my_xch, smem_padded_len(N), tw_s, GroupSync{1 + g, T});
     } else {
       GroupFFT<N, R, NV>::run(v, j, my_xch, smem_padded_len(N), tw_s, WarpSync{});
     }
@@ -274,6 +292,8 @@ int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats) {
   L.chunks = (L.M + L.spc - 1) / L.spc;
   L.grid = ublocks * L.chunks;
   *partial_floats = L.chunks > 1 ? (size_t)L.n_units * L.chunks * np * ((size_t)1 << L.logN) : 0;
+  const long long wbytes = (L.fmt == FMT_I16 ? 4 : 2) * L.nv;
+  L.vec16 = ((L.chan_stride * wbytes) % 16 == 0) && ((reinterpret_cast<uintptr_t>(L.in) & 15) == 0);
   return 0;
 }
 
