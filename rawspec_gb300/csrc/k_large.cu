@@ -173,18 +173,33 @@ k_large_b(LargeLaunch a) {
     }
   }
 
+  if (a.chunks > 1) {
 #pragma unroll
-  for (int m = 0; m < R; ++m) {
-    const int f = k2 + N2 * (j + m * T);
+    for (int m = 0; m < R; ++m)
 #pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      if (a.chunks > 1) {
-        a.partial[(((size_t)unit * a.chunks + chunk) * NP + p) * N + f] = acc[m][p];
-      } else {
-        float* dst = a.out + (((size_t)d * NP + p) * a.Nc + c) * N + out_pos(f, N, a.inverse);
-        if (a.mode == ACC_ADD) *dst = __fmaf_rn(acc[m][p], a.scale, *dst); else *dst = acc[m][p] * a.scale;
-      }
-    }
+      for (int p = 0; p < NP; ++p)
+        a.partial[(((size_t)unit * a.chunks + chunk) * NP + p) * N + k2 + N2 * (j + m * T)] = acc[m][p];
+    return;
+  }
+  float* obase = a.out + ((size_t)d * NP * a.Nc + c) * N;
+  const size_t plane = (size_t)a.Nc * N;
+  if (a.mode == ACC_ADD) {
+    // request every old value before the first store
+    float old[R][NP];
+#pragma unroll
+    for (int m = 0; m < R; ++m)
+#pragma unroll
+      for (int p = 0; p < NP; ++p) old[m][p] = __ldcg(obase + p * plane + out_pos(k2 + N2 * (j + m * T), N, a.inverse));
+#pragma unroll
+    for (int m = 0; m < R; ++m)
+#pragma unroll
+      for (int p = 0; p < NP; ++p)
+        obase[p * plane + out_pos(k2 + N2 * (j + m * T), N, a.inverse)] = __fmaf_rn(acc[m][p], a.scale, old[m][p]);
+  } else {
+#pragma unroll
+    for (int m = 0; m < R; ++m)
+#pragma unroll
+      for (int p = 0; p < NP; ++p) obase[p * plane + out_pos(k2 + N2 * (j + m * T), N, a.inverse)] = acc[m][p] * a.scale;
   }
 }
 

@@ -267,21 +267,38 @@ k_large_fused(LargeLaunch a) {
 #pragma unroll
         for (int m = 0; m < R; ++m) v[q][m] = ld_f2_hint(src + (size_t)q * N2 * N1 + m * T, pol_first);
       GroupFFT<N1, R, NV>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
+      // Detection and store, MC bins at a time: in accumulate mode the MC*NP
+      // old values are all requested before the first store.
+      constexpr int MC = NP == 1 ? R : 4;
+      float* obase = a.out + ((size_t)d * NP * a.Nc + c) * N;
+      const size_t plane = (size_t)a.Nc * N;
 #pragma unroll
-      for (int m = 0; m < R; ++m) {
-        float2 x[NV];
+      for (int m0 = 0; m0 < R; m0 += MC) {
+        float old[MC][NP];
+        if (a.mode == ACC_ADD) {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) x[q] = v[q][m];
-        float acc[NP];
+          for (int mm = 0; mm < MC; ++mm) {
+            const int pos = out_pos(k2 + N2 * (j + (m0 + mm) * T), N, a.inverse);
 #pragma unroll
-        for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
-        detect_acc<POL, NV>(acc, x, im_sign);
-        const int f = k2 + N2 * (j + m * T);
+            for (int p = 0; p < NP; ++p) old[mm][p] = ld_f_hint(obase + p * plane + pos, pol_first);
+          }
+        }
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          float* o = a.out + (((size_t)d * NP + p) * a.Nc + c) * N + out_pos(f, N, a.inverse);
-          const float val = a.mode == ACC_ADD ? __fmaf_rn(acc[p], a.scale, ld_f_hint(o, pol_first)) : acc[p] * a.scale;
-          st_f_hint(o, val, pol_first);
+        for (int mm = 0; mm < MC; ++mm) {
+          const int m = m0 + mm;
+          float2 x[NV];
+#pragma unroll
+          for (int q = 0; q < NV; ++q) x[q] = v[q][m];
+          float acc[NP];
+#pragma unroll
+          for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
+          detect_acc<POL, NV>(acc, x, im_sign);
+          const int pos = out_pos(k2 + N2 * (j + m * T), N, a.inverse);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float val = a.mode == ACC_ADD ? __fmaf_rn(acc[p], a.scale, old[mm][p]) : acc[p] * a.scale;
+            st_f_hint(obase + p * plane + pos, val, pol_first);
+          }
         }
       }
       publish(doneB + slab);
@@ -342,6 +359,8 @@ bool large_fused_supported(const LargeLaunch& L) {
 }
 
 int large_fused_ring() { return kRingSlots; }
+
+int large_fused_row_radix(int pol) { return pol == POL_TP ? fused_rb<POL_TP>() : fused_rb<POL_FULL>(); }
 
 int large_fused_ctl_ints(const LargeLaunch& L) { return 2 + 2 * L.Nc * L.Nss; }
 
