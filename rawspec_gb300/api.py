@@ -168,8 +168,11 @@ class Spectrometer:
         self.dumps: list[list[np.ndarray]] = [[] for _ in products]
         self.ics: list[list[np.ndarray]] = [[] for _ in products]
         self.events: list[tuple[int, int]] = []
+        # With collect=False no callback is installed (as a client without
+        # writers would do); the library then queues no host functions.
         self._cb = DUMP_CALLBACK(self._on_dump)
-        self.ctx.dump_callback = self._cb
+        if collect:
+            self.ctx.dump_callback = self._cb
         rc = self.lib.rawspec_initialize(C.byref(self.ctx))
         if rc != 0:
             raise RuntimeError(f"rawspec_initialize failed ({rc})")

@@ -792,14 +792,17 @@ int rawspec_start_processing(rawspec_context* ctx, int fft_dir) {
         RSG_CUDA(ics_launch(I, g->stream));
         g->launches++;
       }
-      RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
+      // Host functions are queued only when a callback is installed (a NULL
+      // callback would be a no-op on the callback thread anyway).
+      const bool cb = ctx->dump_callback != nullptr;
+      if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
       {
         ProfScope ps(g, RAWSPEC_GB300_K_D2H);
         RSG_CUDA(cudaMemcpyAsync(ctx->h_pwrbuf[i], P.d_out, P.out_bytes, cudaMemcpyDeviceToHost, g->stream));
         if (ctx->incoherently_sum)
           RSG_CUDA(cudaMemcpyAsync(ctx->h_icsbuf[i], P.d_ics, P.ics_bytes, cudaMemcpyDeviceToHost, g->stream));
       }
-      RSG_CUDA(cudaLaunchHostFunc(g->stream, post_dump_fn, &g->cb[i]));
+      if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, post_dump_fn, &g->cb[i]));
     }
   }
   return 0;
@@ -835,7 +838,8 @@ unsigned int rawspec_check_for_completion(rawspec_context* ctx) {
 int rawspec_wait_for_completion(rawspec_context* ctx) {
   GpuCtx* g = G(ctx);
   if (!g) return 1;
-  for (unsigned i = 0; i < ctx->No; i++) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
+  if (ctx->dump_callback)
+    for (unsigned i = 0; i < ctx->No; i++) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) return 1;
   for (unsigned i = 0; i < ctx->No; i++) {
     if (!g->prod[i].d_ctl) continue;
