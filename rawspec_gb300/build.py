@@ -44,15 +44,20 @@ def _deps() -> list[Path]:
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or _extra_flags():
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps())
 
 
+def _extra_flags() -> list[str]:
+    """Tuning definitions from RAWSPEC_NVCC_FLAGS (e.g. "-DRSG_FUSED_TP_MINB=2")."""
+    return os.environ.get("RAWSPEC_NVCC_FLAGS", "").split()
+
+
 def _compile(src: Path, verbose: bool) -> Path:
     obj = BUILD / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *_extra_flags(), "-c", str(src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), flush=True)
     res = subprocess.run(cmd, capture_output=True, text=True)

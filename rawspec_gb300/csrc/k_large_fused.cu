@@ -28,7 +28,6 @@ namespace rsg {
 namespace {
 
 constexpr int kFusedTPB = 256;
-constexpr int kFusedMinBlocks = 2;
 constexpr int kRingSlots = 4;
 constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
 
@@ -36,6 +35,16 @@ constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
 // all modes run at radix 16.
 template <int POL>
 __host__ __device__ constexpr int fused_rb() { return 16; }
+
+// Resident CTAs per SM the register budget is set for: the polarisations are
+// transformed one after the other (16 complex values per thread), which
+// leaves room for three CTAs in total-power mode; the cross-pol modes keep the
+// first polarisation's spectrum while the second is transformed.
+#ifndef RSG_FUSED_TP_MINB
+#define RSG_FUSED_TP_MINB 3
+#endif
+template <int POL>
+__host__ __device__ constexpr int fused_minb() { return POL == POL_TP ? RSG_FUSED_TP_MINB : 2; }
 
 // Shared-memory distance between the exchange buffers of neighbouring
 // interleaved sub-FFTs, chosen so that the C sub-FFTs served by one
@@ -54,7 +63,7 @@ struct FusedCfg {
   static constexpr int RB = fused_rb<POL>(), TB = N1 / RB, CB = kFusedTPB / TB;
   static constexpr int TWA = stockham_tw_size(N2, RA), TWB = stockham_tw_size(N1, RB);
   static constexpr int TWA2 = (TWA + 1) & ~1, TWB2 = (TWB + 1) & ~1;
-  static constexpr int GSA = group_stride(N2, NV, CA), GSB = group_stride(N1, NV, CB);
+  static constexpr int GSA = group_stride(N2, 1, CA), GSB = group_stride(N1, 1, CB);
   static constexpr int XCH = CA * GSA > CB * GSB ? CA * GSA : CB * GSB;
   static constexpr size_t SMEM = (size_t)(TWA2 + TWB2 + XCH) * sizeof(float2);
   static_assert(TA * CA == kFusedTPB && TB * CB == kFusedTPB, "sub-FFT threads must tile the CTA");
@@ -155,7 +164,7 @@ struct HintLoad<uint16_t> {
 }  // namespace
 
 template <int N1, int N2, int FMT, int NV, int POL>
-__global__ void __launch_bounds__(kFusedTPB, kFusedMinBlocks)
+__global__ void __launch_bounds__(kFusedTPB, fused_minb<POL>())
 k_large_fused(LargeLaunch a) {
   using F = FusedCfg<N1, N2, NV, POL>;
   constexpr int N = N1 * N2;
@@ -225,30 +234,29 @@ k_large_fused(LargeLaunch a) {
       using W = typename SampleWord<FMT, NV>::type;
       const W* src = reinterpret_cast<const W*>(a.in) + (long long)c * a.chan_stride + (long long)sp * N + n1 +
                      (long long)N1 * j;
-      float2 v[NV][R];
-      {
-        W w[R];
+      W w[R];
 #pragma unroll
-        for (int m = 0; m < R; ++m) w[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
+      for (int m = 0; m < R; ++m) w[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
+      const int e0 = n1 * j;
+      const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
+      float2* dst = scr + n1;
+      const float2* twm = a.twM + n1;
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        float2 v[1][R];
 #pragma unroll
         for (int m = 0; m < R; ++m) {
           float2 smp[NV];
           Unpack<FMT, NV>::run(w[m], smp);
-#pragma unroll
-          for (int q = 0; q < NV; ++q) v[q][m] = smp[q];
+          v[0][m] = q == 0 ? smp[0] : smp[NV - 1];
         }
-      }
-      const int e0 = n1 * j;
-      const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
-      GroupFFT<N2, R, NV>::run(v, j, xch + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
-      float2* dst = scr + n1;
-      const float2* twm = a.twM + n1;
+        GroupFFT<N2, R, 1>::run(v, j, xch + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
 #pragma unroll
-      for (int m = 0; m < R; ++m) {
-        const int k2 = j + m * T;
-        const float2 w = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
-#pragma unroll
-        for (int q = 0; q < NV; ++q) st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[q][m], w), pol_last);
+        for (int m = 0; m < R; ++m) {
+          const int k2 = j + m * T;
+          const float2 w = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
+          st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[0][m], w), pol_last);
+        }
       }
       publish(doneA + slab);
     } else {
@@ -261,12 +269,31 @@ k_large_fused(LargeLaunch a) {
       const int c = slab / a.units_per_chan;
       const int d = slab % a.units_per_chan;
       const float2* src = scr + (size_t)k2 * N1 + j;
-      float2 v[NV][R];
+      // Polarisation 0, then 1; total power accumulates |X|^2 of each, the
+      // cross-pol modes keep X0 while X1 is transformed.
+      float2 x0[NV == 2 && POL != POL_TP ? R : 1];
+      float tp[POL == POL_TP ? R : 1];
+      float2 v[1][R];
 #pragma unroll
-      for (int q = 0; q < NV; ++q)
+      for (int q = 0; q < NV; ++q) {
 #pragma unroll
-        for (int m = 0; m < R; ++m) v[q][m] = ld_f2_hint(src + (size_t)q * N2 * N1 + m * T, pol_first);
-      GroupFFT<N1, R, NV>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
+        for (int m = 0; m < R; ++m) v[0][m] = ld_f2_hint(src + (size_t)q * N2 * N1 + m * T, pol_first);
+        GroupFFT<N1, R, 1>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
+        if constexpr (POL == POL_TP) {
+#pragma unroll
+          for (int m = 0; m < R; ++m) {
+            float t1[1] = {q == 0 ? 0.0f : tp[m]};
+            const float2 xx[1] = {v[0][m]};
+            detect_acc<POL_TP, 1>(t1, xx, im_sign);
+            tp[m] = t1[0];
+          }
+        } else {
+          if (q == 0) {
+#pragma unroll
+            for (int m = 0; m < R; ++m) x0[m] = v[0][m];
+          }
+        }
+      }
       // Detection and store, MC bins at a time: in accumulate mode the MC*NP
       // old values are all requested before the first store.
       constexpr int MC = NP == 1 ? R : 4;
@@ -286,13 +313,15 @@ k_large_fused(LargeLaunch a) {
 #pragma unroll
         for (int mm = 0; mm < MC; ++mm) {
           const int m = m0 + mm;
-          float2 x[NV];
-#pragma unroll
-          for (int q = 0; q < NV; ++q) x[q] = v[q][m];
           float acc[NP];
+          if constexpr (POL == POL_TP) {
+            acc[0] = tp[m];
+          } else {
 #pragma unroll
-          for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
-          detect_acc<POL, NV>(acc, x, im_sign);
+            for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
+            const float2 x[2] = {x0[m], v[0][m]};
+            detect_acc<POL, 2>(acc, x, im_sign);
+          }
           const int pos = out_pos(k2 + N2 * (j + m * T), N, a.inverse);
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
