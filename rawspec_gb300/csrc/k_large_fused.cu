@@ -29,6 +29,10 @@ namespace {
 
 constexpr int kFusedTPB = 256;
 constexpr int kRingSlots = 4;
+#ifndef RSG_FUSED_K
+#define RSG_FUSED_K 4
+#endif
+constexpr int kTilesPerItem = RSG_FUSED_K;  // tiles per work item (amortises the item overheads)
 constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
 
 // Row tiles hold no multi-spectrum accumulators (one spectrum per unit), so
@@ -41,7 +45,7 @@ __host__ __device__ constexpr int fused_rb() { return 16; }
 // leaves room for three CTAs in total-power mode; the cross-pol modes keep the
 // first polarisation's spectrum while the second is transformed.
 #ifndef RSG_FUSED_TP_MINB
-#define RSG_FUSED_TP_MINB 3
+#define RSG_FUSED_TP_MINB 2
 #endif
 template <int POL>
 __host__ __device__ constexpr int fused_minb() { return POL == POL_TP ? RSG_FUSED_TP_MINB : 2; }
@@ -102,11 +106,11 @@ __device__ __forceinline__ void wait_count(const int* cnt, int target, int* err,
 // counted: the CTA barrier orders every thread's writes before thread 0's
 // device-scope fence and release of the counter (the same pattern as a grid
 // barrier).
-__device__ __forceinline__ void publish(int* cnt) {
+__device__ __forceinline__ void publish(int* cnt, int tiles) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    atomicAdd(cnt, 1);
+    atomicAdd(cnt, tiles);
   }
 }
 
@@ -182,7 +186,10 @@ k_large_fused(LargeLaunch a) {
 
   const int S = a.S;
   constexpr int tilesA = N1 / F::CA, tilesB = N2 / F::CB;
-  const long long total = (long long)S * (tilesA + tilesB);
+  constexpr int K = kTilesPerItem;
+  static_assert(tilesA % K == 0 && tilesB % K == 0, "items must cover whole tiles");
+  constexpr int itemsA = tilesA / K, itemsB = tilesB / K;
+  const long long total = (long long)S * (itemsA + itemsB);
   int* err = a.ctl;       // sticky error word (never reset by a launch)
   int* next = a.ctl + 1;
   int* doneA = a.ctl + 2;
@@ -198,25 +205,26 @@ k_large_fused(LargeLaunch a) {
     __syncthreads();
     if (item >= total) break;
 
-    // Decode the item: A(0) | [A(k) B(k-1)] for k = 1..S-1 | B(S-1).
+    // Decode the item: A(0) | [A(k) B(k-1)] for k = 1..S-1 | B(S-1); each
+    // item covers K consecutive tiles of one slab.
     bool isA;
-    int slab, tile;
-    if (item < tilesA) {
+    int slab, titem;
+    if (item < itemsA) {
       isA = true;
       slab = 0;
-      tile = (int)item;
+      titem = (int)item;
     } else {
-      const long long j = item - tilesA;
-      const int k = (int)(j / (tilesA + tilesB)) + 1;
-      const int r = (int)(j % (tilesA + tilesB));
-      if (k <= S - 1 && r < tilesA) {
+      const long long j = item - itemsA;
+      const int k = (int)(j / (itemsA + itemsB)) + 1;
+      const int r = (int)(j % (itemsA + itemsB));
+      if (k <= S - 1 && r < itemsA) {
         isA = true;
         slab = k;
-        tile = r;
+        titem = r;
       } else {
         isA = false;
         slab = k - 1;
-        tile = k <= S - 1 ? r - tilesA : r;
+        titem = k <= S - 1 ? r - itemsA : r;
       }
     }
     const int slot = slab % a.ring;
@@ -224,113 +232,132 @@ k_large_fused(LargeLaunch a) {
 
     if (isA) {
       if (slab >= a.ring) wait_count(doneB + (slab - a.ring), tilesB, err, 1);
-      // ---- column tile: N2-point FFTs of C_A columns n1 --------------------
+      // ---- K column tiles: N2-point FFTs of C_A columns n1 each ------------
       constexpr int R = F::RA, T = F::TA, C = F::CA;
       const int col = tid % C;
       const int j = tid / C;
-      const int n1 = tile * C + col;
       const int c = slab / a.Nss;
       const int sp = slab % a.Nss;
       using W = typename SampleWord<FMT, NV>::type;
-      const W* src = reinterpret_cast<const W*>(a.in) + (long long)c * a.chan_stride + (long long)sp * N + n1 +
-                     (long long)N1 * j;
+      const W* src0 = reinterpret_cast<const W*>(a.in) + (long long)c * a.chan_stride + (long long)sp * N + col +
+                      (long long)N1 * j;
       W w[R];
+      {
+        const W* src = src0 + titem * K * C;
 #pragma unroll
-      for (int m = 0; m < R; ++m) w[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
-      const int e0 = n1 * j;
-      const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
-      float2* dst = scr + n1;
-      const float2* twm = a.twM + n1;
+        for (int m = 0; m < R; ++m) w[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
+      }
+#pragma unroll 1
+      for (int t = 0; t < K; ++t) {
+        const int n1 = (titem * K + t) * C + col;
+        W wn[R];  // next tile's samples, requested before this tile's FFTs
+        if (t + 1 < K) {
+          const W* src = src0 + (titem * K + t + 1) * C;
 #pragma unroll
-      for (int q = 0; q < NV; ++q) {
-        float2 v[1][R];
-#pragma unroll
-        for (int m = 0; m < R; ++m) {
-          float2 smp[NV];
-          Unpack<FMT, NV>::run(w[m], smp);
-          v[0][m] = q == 0 ? smp[0] : smp[NV - 1];
+          for (int m = 0; m < R; ++m) wn[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
         }
-        GroupFFT<N2, R, 1>::run(v, j, xch + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
+        const int e0 = n1 * j;
+        const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
+        float2* dst = scr + n1;
+        const float2* twm = a.twM + n1;
 #pragma unroll
-        for (int m = 0; m < R; ++m) {
-          const int k2 = j + m * T;
-          const float2 w = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
-          st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[0][m], w), pol_last);
+        for (int q = 0; q < NV; ++q) {
+          float2 v[1][R];
+#pragma unroll
+          for (int m = 0; m < R; ++m) {
+            float2 smp[NV];
+            Unpack<FMT, NV>::run(w[m], smp);
+            v[0][m] = q == 0 ? smp[0] : smp[NV - 1];
+          }
+          GroupFFT<N2, R, 1>::run(v, j, xch + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
+#pragma unroll
+          for (int m = 0; m < R; ++m) {
+            const int k2 = j + m * T;
+            const float2 tw = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
+            st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[0][m], tw), pol_last);
+          }
+        }
+        if (t + 1 < K) {
+#pragma unroll
+          for (int m = 0; m < R; ++m) w[m] = wn[m];
         }
       }
-      publish(doneA + slab);
+      publish(doneA + slab, K);
     } else {
       wait_count(doneA + slab, tilesA, err, 2);
-      // ---- row tile: N1-point FFTs of C_B rows k2, detection, store -------
+      // ---- K row tiles: N1-point FFTs of C_B rows k2, detection, store ----
       constexpr int R = F::RB, T = F::TB, C = F::CB;
       const int row = tid % C;
       const int j = tid / C;
-      const int k2 = tile * C + row;
       const int c = slab / a.units_per_chan;
       const int d = slab % a.units_per_chan;
-      const float2* src = scr + (size_t)k2 * N1 + j;
-      // Polarisation 0, then 1; total power accumulates |X|^2 of each, the
-      // cross-pol modes keep X0 while X1 is transformed.
-      float2 x0[NV == 2 && POL != POL_TP ? R : 1];
-      float tp[POL == POL_TP ? R : 1];
-      float2 v[1][R];
-#pragma unroll
-      for (int q = 0; q < NV; ++q) {
-#pragma unroll
-        for (int m = 0; m < R; ++m) v[0][m] = ld_f2_hint(src + (size_t)q * N2 * N1 + m * T, pol_first);
-        GroupFFT<N1, R, 1>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
-        if constexpr (POL == POL_TP) {
-#pragma unroll
-          for (int m = 0; m < R; ++m) {
-            float t1[1] = {q == 0 ? 0.0f : tp[m]};
-            const float2 xx[1] = {v[0][m]};
-            detect_acc<POL_TP, 1>(t1, xx, im_sign);
-            tp[m] = t1[0];
-          }
-        } else {
-          if (q == 0) {
-#pragma unroll
-            for (int m = 0; m < R; ++m) x0[m] = v[0][m];
-          }
-        }
-      }
-      // Detection and store, MC bins at a time: in accumulate mode the MC*NP
-      // old values are all requested before the first store.
-      constexpr int MC = NP == 1 ? R : 4;
       float* obase = a.out + ((size_t)d * NP * a.Nc + c) * N;
       const size_t plane = (size_t)a.Nc * N;
+#pragma unroll 1
+      for (int t = 0; t < K; ++t) {
+        const int k2 = (titem * K + t) * C + row;
+        const float2* src = scr + (size_t)k2 * N1 + j;
+        // Polarisation 0, then 1; total power accumulates |X|^2 of each, the
+        // cross-pol modes keep X0 while X1 is transformed.
+        float2 x0[NV == 2 && POL != POL_TP ? R : 1];
+        float tp[POL == POL_TP ? R : 1];
+        float2 v[1][R];
 #pragma unroll
-      for (int m0 = 0; m0 < R; m0 += MC) {
-        float old[MC][NP];
-        if (a.mode == ACC_ADD) {
+        for (int q = 0; q < NV; ++q) {
 #pragma unroll
-          for (int mm = 0; mm < MC; ++mm) {
-            const int pos = out_pos(k2 + N2 * (j + (m0 + mm) * T), N, a.inverse);
+          for (int m = 0; m < R; ++m) v[0][m] = ld_f2_hint(src + (size_t)q * N2 * N1 + m * T, pol_first);
+          GroupFFT<N1, R, 1>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
+          if constexpr (POL == POL_TP) {
 #pragma unroll
-            for (int p = 0; p < NP; ++p) old[mm][p] = ld_f_hint(obase + p * plane + pos, pol_first);
+            for (int m = 0; m < R; ++m) {
+              float t1[1] = {q == 0 ? 0.0f : tp[m]};
+              const float2 xx[1] = {v[0][m]};
+              detect_acc<POL_TP, 1>(t1, xx, im_sign);
+              tp[m] = t1[0];
+            }
+          } else {
+            if (q == 0) {
+#pragma unroll
+              for (int m = 0; m < R; ++m) x0[m] = v[0][m];
+            }
           }
         }
+        // Detection and store, MC bins at a time: in accumulate mode the
+        // MC*NP old values are all requested before the first store.
+        constexpr int MC = NP == 1 ? 8 : 4;
 #pragma unroll
-        for (int mm = 0; mm < MC; ++mm) {
-          const int m = m0 + mm;
-          float acc[NP];
-          if constexpr (POL == POL_TP) {
-            acc[0] = tp[m];
-          } else {
+        for (int m0 = 0; m0 < R; m0 += MC) {
+          float old[MC][NP];
+          if (a.mode == ACC_ADD) {
 #pragma unroll
-            for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
-            const float2 x[2] = {x0[m], v[0][m]};
-            detect_acc<POL, 2>(acc, x, im_sign);
+            for (int mm = 0; mm < MC; ++mm) {
+              const int pos = out_pos(k2 + N2 * (j + (m0 + mm) * T), N, a.inverse);
+#pragma unroll
+              for (int p = 0; p < NP; ++p) old[mm][p] = ld_f_hint(obase + p * plane + pos, pol_first);
+            }
           }
-          const int pos = out_pos(k2 + N2 * (j + m * T), N, a.inverse);
 #pragma unroll
-          for (int p = 0; p < NP; ++p) {
-            const float val = a.mode == ACC_ADD ? __fmaf_rn(acc[p], a.scale, old[mm][p]) : acc[p] * a.scale;
-            st_f_hint(obase + p * plane + pos, val, pol_first);
+          for (int mm = 0; mm < MC; ++mm) {
+            const int m = m0 + mm;
+            float acc[NP];
+            if constexpr (POL == POL_TP) {
+              acc[0] = tp[m];
+            } else {
+#pragma unroll
+              for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
+              const float2 x[2] = {x0[m], v[0][m]};
+              detect_acc<POL, 2>(acc, x, im_sign);
+            }
+            const int pos = out_pos(k2 + N2 * (j + m * T), N, a.inverse);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+              const float val = a.mode == ACC_ADD ? __fmaf_rn(acc[p], a.scale, old[mm][p]) : acc[p] * a.scale;
+              st_f_hint(obase + p * plane + pos, val, pol_first);
+            }
           }
         }
       }
-      publish(doneB + slab);
+      publish(doneB + slab, K);
     }
   }
 }
