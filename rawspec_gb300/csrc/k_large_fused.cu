@@ -3,9 +3,10 @@
 // the 2^20-point product of the production configuration).
 //
 // The two passes of the four-step FFT (see k_large.cu) become work items of
-// one persistent kernel, taken in a fixed order through an atomic counter:
+// one persistent kernel, taken in a fixed order through an atomic counter
+// (here with a lag of 2):
 //
-//   A(0) A(1) B(0) A(2) B(1) ... A(S-1) B(S-2) B(S-1)
+//   A(0) A(1) A(2) B(0) A(3) B(1) ... A(S-1) B(S-3) B(S-2) B(S-1)
 //
 // where A(s) are the column tiles of slab s (one channel-spectrum, both
 // polarisations) and B(s) its row tiles.  A(s) writes the FP32 intermediate
@@ -28,9 +29,21 @@ namespace rsg {
 namespace {
 
 constexpr int kFusedTPB = 256;
-constexpr int kRingSlots = 4;
+#ifndef RSG_FUSED_LAG
+#define RSG_FUSED_LAG 2
+#endif
+#ifndef RSG_FUSED_RING
+#define RSG_FUSED_RING 4
+#endif
+// Row tiles of slab s are queued after the column tiles of slab s + kLag, so
+// that a row tile rarely finds its slab's column tiles still running; a slot
+// of the intermediate ring is reused kRingSlots slabs later (> kLag keeps
+// every wait pointed at earlier items).
+constexpr int kLag = RSG_FUSED_LAG;
+constexpr int kRingSlots = RSG_FUSED_RING;
+static_assert(kRingSlots > kLag, "a slot must be released by row tiles queued before its next column tiles");
 #ifndef RSG_FUSED_K
-#define RSG_FUSED_K 4
+#define RSG_FUSED_K 2
 #endif
 constexpr int kTilesPerItem = RSG_FUSED_K;  // tiles per work item (amortises the item overheads)
 constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
@@ -205,26 +218,31 @@ k_large_fused(LargeLaunch a) {
     __syncthreads();
     if (item >= total) break;
 
-    // Decode the item: A(0) | [A(k) B(k-1)] for k = 1..S-1 | B(S-1); each
-    // item covers K consecutive tiles of one slab.
+    // Decode the item.  Segment k holds A(k) (k < S) followed by B(k - lag)
+    // (k >= lag); each item covers K consecutive tiles of one slab.
     bool isA;
     int slab, titem;
-    if (item < itemsA) {
-      isA = true;
-      slab = 0;
-      titem = (int)item;
-    } else {
-      const long long j = item - itemsA;
-      const int k = (int)(j / (itemsA + itemsB)) + 1;
-      const int r = (int)(j % (itemsA + itemsB));
-      if (k <= S - 1 && r < itemsA) {
+    {
+      const int p1 = S < kLag ? S : kLag;                 // A-only segments
+      const int mid = S > kLag ? S - kLag : 0;            // A+B segments
+      const long long n1 = (long long)p1 * itemsA;
+      const long long n2 = (long long)mid * (itemsA + itemsB);
+      if (item < n1) {
         isA = true;
-        slab = k;
-        titem = r;
-      } else {
+        slab = (int)(item / itemsA);
+        titem = (int)(item % itemsA);
+      } else if (item < n1 + n2) {
+        const long long i2 = item - n1;
+        const int k = kLag + (int)(i2 / (itemsA + itemsB));
+        const int r = (int)(i2 % (itemsA + itemsB));
+        isA = r < itemsA;
+        slab = isA ? k : k - kLag;
+        titem = isA ? r : r - itemsA;
+      } else {                                            // B-only tail
+        const long long i3 = item - n1 - n2;
         isA = false;
-        slab = k - 1;
-        titem = k <= S - 1 ? r - itemsA : r;
+        slab = mid + (int)(i3 / itemsB);
+        titem = (int)(i3 % itemsB);
       }
     }
     const int slot = slab % a.ring;
