@@ -11,9 +11,10 @@ Metric: RAW-in GB/s (RAW bytes of the step / step time).
   value  device-resident throughput: the buffer is in HBM, the timed region
          is K x rawspec_start_processing (kernels + dumps to pinned host
          memory), timed with CUDA events on the library's stream;
-  e2e    through the C-ABI from pinned host blocks: K x
-         (rawspec_copy_blocks_to_gpu + rawspec_start_processing +
-         rawspec_wait_for_completion), wall clock.
+  e2e    through the C-ABI from pinned host blocks, the reference CLI's
+         per-buffer sequence: K x (rawspec_wait_for_completion +
+         rawspec_copy_blocks_to_gpu_and_start_processing), then a final
+         wait; wall clock.
 
 `--impl reference` times the CPU restatement of the same chain (the
 reference has no CPU implementation of its spectrometer; the OpenMP FP32
@@ -229,20 +230,20 @@ def run_native(args, rank, world, local_rank):
         spec.set_profiling(False)
         # end-to-end through the C-ABI from pinned host blocks
         for _ in range(max(1, args.warmup // 2)):
-            spec.copy_to_gpu()
-            spec.start()
+            spec.copy_and_start()
             spec.wait()
         sizes = [spec.ctx.h_pwrbuf_size[i] for i in range(3)]
         nis = [spec.product_info(i)[1] for i in range(3)]
         barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            if lib.rawspec_copy_blocks_to_gpu(cp, 0, 0, 2) != 0:
-                raise RuntimeError("copy failed")
-            if lib.rawspec_start_processing(cp, 1) != 0:
-                raise RuntimeError("start_processing failed")
+            # the reference CLI's per-buffer sequence (rawspec.c:1012-1014)
             if lib.rawspec_wait_for_completion(cp) != 0:
                 raise RuntimeError("wait failed")
+            if lib.rawspec_copy_blocks_to_gpu_and_start_processing(cp, 2, 0, 1) != 0:
+                raise RuntimeError("copy/start failed")
+        if lib.rawspec_wait_for_completion(cp) != 0:
+            raise RuntimeError("wait failed")
         e2e_s = max_over_ranks(time.perf_counter() - t0)
         # device->host dump bytes per step (dump schedule over the timed steps)
         start = args.warmup + max(1, args.warmup // 2) + args.steps

@@ -228,15 +228,26 @@ class Spectrometer:
     def wait(self) -> int:
         return self.lib.rawspec_wait_for_completion(C.byref(self.ctx))
 
-    def process(self, blocks: np.ndarray, fft_dir: int = RAWSPEC_FORWARD_FFT) -> None:
-        """Feeds every complete buffer (Nb blocks) of `blocks` through the library."""
+    def copy_and_start(self, fft_dir: int = RAWSPEC_FORWARD_FFT) -> None:
+        """rawspec_copy_blocks_to_gpu_and_start_processing, as the reference CLI calls it."""
+        rc = self.lib.rawspec_copy_blocks_to_gpu_and_start_processing(C.byref(self.ctx), self.Nb,
+                                                                        1 if self.nbits_in == 4 else 0, fft_dir)
+        if rc != 0:
+            raise RuntimeError("rawspec_copy_blocks_to_gpu_and_start_processing failed")
+
+    def process(self, blocks: np.ndarray, fft_dir: int = RAWSPEC_FORWARD_FFT, combined: bool = False) -> None:
+        """Feeds every complete buffer (Nb blocks) of `blocks` through the library
+        (separate copy and start calls, or the combined call of the CLI)."""
         nb = self.Nb
         for b0 in range(0, blocks.shape[0] - nb + 1, nb):
             if self.wait() != 0:
                 raise RuntimeError("wait_for_completion reported an error")
             self.load_blocks(blocks[b0:b0 + nb])
-            self.copy_to_gpu(nb)
-            self.start(fft_dir)
+            if combined:
+                self.copy_and_start(fft_dir)
+            else:
+                self.copy_to_gpu(nb)
+                self.start(fft_dir)
         if self.wait() != 0:
             raise RuntimeError("wait_for_completion reported an error")
 

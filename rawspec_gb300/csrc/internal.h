@@ -46,6 +46,7 @@ struct SmallLaunch {
   int mode = ACC_WRITE, inverse = 0, conj = 0;
   float scale = 1.0f;         // SNORM scale squared, applied to the results
   int vec16 = 0;              // spectra start on 16-byte boundaries (set by small_configure)
+  int unit0 = 0, unit_count = 0;  // units of this launch (a channel range; all by default)
 };
 
 // Chooses block size, units per block and chunks per unit.  target_ctas is
@@ -64,6 +65,7 @@ struct FinalizeLaunch {
   int n_units = 0, chunks = 0, np = 1, N = 0, Nc = 0, units_per_chan = 0;
   int mode = ACC_WRITE, inverse = 0;
   float scale = 1.0f;
+  int unit0 = 0;              // first unit; n_units counts the units of this launch
 };
 cudaError_t finalize_launch(const FinalizeLaunch& L, cudaStream_t s);
 
@@ -93,7 +95,9 @@ struct LargeLaunch {
   int mode = ACC_WRITE, inverse = 0, conj = 0;
   float scale = 1.0f;
   // persistent fused kernel (one spectrum per integration unit)
-  int S = 0;                      // slabs per buffer (Nc * Nss)
+  int S = 0;                      // slabs of this launch (Nc * Nss for a whole buffer)
+  int slab0 = 0;                  // first slab of this launch
+  int unit0 = 0, unit_count = 0;  // units of this launch (two-kernel path)
   int ring = 0;                   // intermediate slots
   int* ctl = nullptr;             // [0] error, [1] item counter, [2..2+S) A done, [2+S..2+2S) B done
   int fused_ctas = 0;             // persistent grid size
@@ -139,6 +143,7 @@ struct Expand4Launch {
   const uint8_t* packed = nullptr;  // [Nc][Nb*blk_bytes_packed]
   int8_t* out = nullptr;            // [Nc][Nb*blk_bytes_packed*2]
   int Nc = 0, Nb = 0;
+  int c0 = 0, nch = -1;             // channel range (nch < 0: all channels)
   long long blk_bytes_packed = 0;   // Ntpb * Np
   int dst_block = 0, num_blocks = 0;
 };

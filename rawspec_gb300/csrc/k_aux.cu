@@ -91,13 +91,13 @@ __device__ __forceinline__ uint32_t expand2(uint32_t b0, uint32_t b1) {
 __global__ void k_expand4_words(Expand4Launch a) {
   // one thread per 4 packed bytes; blk_bytes_packed % 4 == 0
   const long long words_per_seg = a.blk_bytes_packed / 4;
-  const long long total = words_per_seg * a.Nc * a.num_blocks;
+  const long long total = words_per_seg * a.nch * a.num_blocks;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const long long w = i % words_per_seg;
     const long long seg = i / words_per_seg;
-    const int c = (int)(seg % a.Nc);
-    const int bi = (int)(seg / a.Nc);
+    const int c = a.c0 + (int)(seg % a.nch);
+    const int bi = (int)(seg / a.nch);
     const int blk = (a.dst_block + bi) % a.Nb;
     const long long pin = (long long)c * a.Nb * a.blk_bytes_packed + (long long)blk * a.blk_bytes_packed;
     const uint32_t p = *reinterpret_cast<const uint32_t*>(a.packed + pin + 4 * w);
@@ -109,13 +109,13 @@ __global__ void k_expand4_words(Expand4Launch a) {
 }
 
 __global__ void k_expand4_bytes(Expand4Launch a) {
-  const long long total = a.blk_bytes_packed * a.Nc * a.num_blocks;
+  const long long total = a.blk_bytes_packed * a.nch * a.num_blocks;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const long long b = i % a.blk_bytes_packed;
     const long long seg = i / a.blk_bytes_packed;
-    const int c = (int)(seg % a.Nc);
-    const int bi = (int)(seg / a.Nc);
+    const int c = a.c0 + (int)(seg % a.nch);
+    const int bi = (int)(seg / a.nch);
     const int blk = (a.dst_block + bi) % a.Nb;
     const long long pin = (long long)c * a.Nb * a.blk_bytes_packed + (long long)blk * a.blk_bytes_packed + b;
     const uint8_t v = a.packed[pin];
@@ -124,9 +124,14 @@ __global__ void k_expand4_bytes(Expand4Launch a) {
   }
 }
 
-cudaError_t expand4_launch(const Expand4Launch& L, cudaStream_t s) {
+cudaError_t expand4_launch(const Expand4Launch& Lin, cudaStream_t s) {
+  Expand4Launch L = Lin;
+  if (L.nch < 0) {
+    L.c0 = 0;
+    L.nch = L.Nc;
+  }
   const bool words = (L.blk_bytes_packed % 4) == 0;
-  const long long items = (words ? L.blk_bytes_packed / 4 : L.blk_bytes_packed) * L.Nc * L.num_blocks;
+  const long long items = (words ? L.blk_bytes_packed / 4 : L.blk_bytes_packed) * L.nch * L.num_blocks;
   const int blocks = (int)std::max<long long>(1, std::min<long long>((items + 255) / 256, 152LL * 32));
   if (words) k_expand4_words<<<blocks, 256, 0, s>>>(L);
   else k_expand4_bytes<<<blocks, 256, 0, s>>>(L);

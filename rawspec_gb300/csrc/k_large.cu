@@ -75,7 +75,7 @@ k_large_a(LargeLaunch a) {
   const int N1 = 1 << a.logN1;
   const int tiles = N1 / C;
   const int tile = blockIdx.x % tiles;
-  const int slab = blockIdx.x / tiles;
+  const int slab = a.slab0 + blockIdx.x / tiles;
   const int c = slab / a.Nss;
   const int s = slab % a.Nss;
   const int col = tid % C;
@@ -137,7 +137,7 @@ k_large_b(LargeLaunch a) {
   const int tiles = N2 / C;
   const int tile = blockIdx.x % tiles;
   const int uc = blockIdx.x / tiles;
-  const int unit = uc / a.chunks;
+  const int unit = a.unit0 + uc / a.chunks;
   const int chunk = uc % a.chunks;
   const int c = unit / a.units_per_chan;
   const int d = unit % a.units_per_chan;
@@ -215,7 +215,8 @@ cudaError_t launch_a_t(const LargeLaunch& L, cudaStream_t s, bool prep) {
   const size_t smem = passA_smem<N2, NV>();
   if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int N1 = 1 << L.logN1;
-  const long long grid = (long long)(N1 / Cf::C) * L.Nc * L.Nss;
+  const long long grid = (long long)(N1 / Cf::C) * L.S;
+  if (grid < 1) return cudaSuccess;
   k<<<(unsigned)grid, Cf::TPB, smem, s>>>(L);
   return cudaGetLastError();
 }
@@ -228,7 +229,8 @@ cudaError_t launch_b_t(const LargeLaunch& L, cudaStream_t s, bool prep) {
   const size_t smem = passB_smem<N1, NV, R>();
   if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int N2 = 1 << L.logN2;
-  const long long grid = (long long)(N2 / Cf::C) * L.n_units * L.chunks;
+  const long long grid = (long long)(N2 / Cf::C) * L.unit_count * L.chunks;
+  if (grid < 1) return cudaSuccess;
   k<<<(unsigned)grid, Cf::TPB, smem, s>>>(L);
   return cudaGetLastError();
 }
@@ -312,6 +314,10 @@ int large_configure(LargeLaunch& L, int target_ctas, size_t* scratch_float2, siz
   L.chunks = (L.M + L.spc - 1) / L.spc;
   *scratch_float2 = (size_t)L.Nc * L.Nss * L.nv * ((size_t)1 << L.logN);
   *partial_floats = L.chunks > 1 ? (size_t)L.n_units * L.chunks * np * ((size_t)1 << L.logN) : 0;
+  L.slab0 = 0;
+  L.S = L.Nc * L.Nss;
+  L.unit0 = 0;
+  L.unit_count = L.n_units;
   return 0;
 }
 

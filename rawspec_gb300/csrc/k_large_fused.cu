@@ -254,8 +254,8 @@ k_large_fused(LargeLaunch a) {
       constexpr int R = F::RA, T = F::TA, C = F::CA;
       const int col = tid % C;
       const int j = tid / C;
-      const int c = slab / a.Nss;
-      const int sp = slab % a.Nss;
+      const int c = (a.slab0 + slab) / a.Nss;
+      const int sp = (a.slab0 + slab) % a.Nss;
       using W = typename SampleWord<FMT, NV>::type;
       const W* src0 = reinterpret_cast<const W*>(a.in) + (long long)c * a.chan_stride + (long long)sp * N + col +
                       (long long)N1 * j;
@@ -307,8 +307,8 @@ k_large_fused(LargeLaunch a) {
       constexpr int R = F::RB, T = F::TB, C = F::CB;
       const int row = tid % C;
       const int j = tid / C;
-      const int c = slab / a.units_per_chan;
-      const int d = slab % a.units_per_chan;
+      const int c = (a.slab0 + slab) / a.units_per_chan;
+      const int d = (a.slab0 + slab) % a.units_per_chan;
       float* obase = a.out + ((size_t)d * NP * a.Nc + c) * N;
       const size_t plane = (size_t)a.Nc * N;
 #pragma unroll 1

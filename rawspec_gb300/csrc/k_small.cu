@@ -86,10 +86,10 @@ k_small(SmallLaunch a) {
   const int gi = g % gps;
   const int ublock = blockIdx.x / a.chunks;
   const int chunk = blockIdx.x % a.chunks;
-  const int unit = ublock * a.sets + set;
+  const int unit = a.unit0 + ublock * a.sets + set;
   const int s_begin = chunk * a.spc;
   const int s_end = min(a.M, s_begin + a.spc);
-  const bool unit_ok = unit < a.n_units;
+  const bool unit_ok = unit < a.unit0 + a.unit_count;
   const int c = unit_ok ? unit / a.units_per_chan : 0;
   const int d = unit_ok ? unit % a.units_per_chan : 0;
   const long long chan_base = (long long)c * a.chan_stride;
@@ -192,7 +192,7 @@ __global__ void k_finalize(FinalizeLaunch a) {
     const int k = (int)(i % a.N);
     const long long up = i / a.N;
     const int p = (int)(up % a.np);
-    const int unit = (int)(up / a.np);
+    const int unit = a.unit0 + (int)(up / a.np);
     const float* src = a.partial + ((size_t)unit * a.chunks * a.np + p) * a.N + k;
     float s = 0.0f;
     for (int q = 0; q < a.chunks; ++q) s += src[(size_t)q * a.np * a.N];
@@ -249,7 +249,9 @@ cudaError_t launch_t(const SmallLaunch& L, cudaStream_t s, bool prep) {
   if (prep) {  // preparation call: allow the dynamic shared memory
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
   }
-  k<<<L.grid, SmallCfg<N, PolOut<POL>::NP>::TPB, L.smem, s>>>(L);
+  const int grid = ((L.unit_count + L.sets - 1) / L.sets) * L.chunks;
+  if (grid < 1) return cudaSuccess;
+  k<<<grid, SmallCfg<N, PolOut<POL>::NP>::TPB, L.smem, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -292,6 +294,8 @@ int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats) {
   L.chunks = (L.M + L.spc - 1) / L.spc;
   L.grid = ublocks * L.chunks;
   *partial_floats = L.chunks > 1 ? (size_t)L.n_units * L.chunks * np * ((size_t)1 << L.logN) : 0;
+  L.unit0 = 0;
+  L.unit_count = L.n_units;
   const long long wbytes = (L.fmt == FMT_I16 ? 4 : 2) * L.nv;
   L.vec16 = ((L.chan_stride * wbytes) % 16 == 0) && ((reinterpret_cast<uintptr_t>(L.in) & 15) == 0);
   return 0;

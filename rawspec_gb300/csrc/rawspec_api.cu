@@ -38,6 +38,8 @@ namespace {
 using namespace rsg;
 
 constexpr int kMaxLogN = 24;
+constexpr int kMaxCopyGroups = 8;                     // channel groups of the pipelined copy
+constexpr size_t kMinPipelinedBytes = size_t(16) << 20;  // smaller buffers are copied in one piece
 
 #define RSG_CUDA(call)                                                                   \
   do {                                                                                   \
@@ -80,6 +82,9 @@ struct GpuCtx {
   int device = 0;
   int sm_count = 152;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;     // host-to-device copies of the pipelined path
+  cudaEvent_t ev_ready[8] = {nullptr};    // per channel group: its copy has landed
+  cudaEvent_t ev_free = nullptr;          // the previous buffer no longer needs the input
   void* d_in = nullptr;
   size_t in_bytes = 0;
   uint8_t* d_in4 = nullptr;
@@ -355,11 +360,12 @@ int dev_alloc(GpuCtx* g, T** p, size_t bytes) {
   return 0;
 }
 
-int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int n_units, int chunks, int upc, int mode,
-                    int inverse, float scale) {
+int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int unit0, int n_units, int chunks, int upc,
+                    int mode, int inverse, float scale) {
   FinalizeLaunch F;
   F.partial = g->d_partial;
   F.out = P.d_out;
+  F.unit0 = unit0;
   F.n_units = n_units;
   F.chunks = chunks;
   F.np = P.np;
@@ -375,23 +381,31 @@ int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int n_uni
   return 0;
 }
 
-int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse) {
+// Queues product i's kernels for the channels [c0, c1) of the buffer.
+int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse, int c0, int c1) {
   Product& P = g->prod[i];
   if (!P.large) {
     SmallLaunch L = P.sl;
     L.mode = mode;
     L.inverse = inverse;
+    L.unit0 = c0 * L.units_per_chan;
+    L.unit_count = (c1 - c0) * L.units_per_chan;
     {
       ProfScope ps(g, RAWSPEC_GB300_K_SMALL);
       RSG_CUDA(small_launch(L, g->stream));
       g->launches++;
     }
-    if (L.chunks > 1 && launch_finalize(ctx, g, P, L.n_units, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+    if (L.chunks > 1 &&
+        launch_finalize(ctx, g, P, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
       return 1;
   } else {
     LargeLaunch L = P.ll;
     L.mode = mode;
     L.inverse = inverse;
+    L.slab0 = c0 * L.Nss;
+    L.S = (c1 - c0) * L.Nss;
+    L.unit0 = c0 * L.units_per_chan;
+    L.unit_count = (c1 - c0) * L.units_per_chan;
     if (P.fused) {
       ProfScope ps(g, RAWSPEC_GB300_K_LARGE_FUSED);
       RSG_CUDA(large_fused_launch(L, g->stream));
@@ -408,8 +422,68 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
       RSG_CUDA(large_launch_b(L, g->stream));
       g->launches++;
     }
-    if (L.chunks > 1 && launch_finalize(ctx, g, P, L.n_units, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+    if (L.chunks > 1 &&
+        launch_finalize(ctx, g, P, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
       return 1;
+  }
+  return 0;
+}
+
+// Processes one input buffer: the products' kernels over `ngroups` channel
+// groups (group k waits for ready[k] when given; expand4 expands each
+// group's packed input first), then the dumps of the products whose
+// integration completes.
+int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, const cudaEvent_t* ready,
+                   const Expand4Launch* expand4) {
+  const int inverse = fft_dir <= 0 ? 1 : 0;
+  g->inbuf_count++;
+  int mode[MAX_OUTPUTS];
+  for (unsigned i = 0; i < ctx->No; i++)
+    mode[i] = ((g->inbuf_count - 1) % g->prod[i].Nis == 0) ? ACC_WRITE : ACC_ADD;
+  for (int grp = 0; grp < ngroups; grp++) {
+    const int c0 = (int)((long long)grp * ctx->Nc / ngroups);
+    const int c1 = (int)((long long)(grp + 1) * ctx->Nc / ngroups);
+    if (c1 <= c0) continue;
+    if (ready) RSG_CUDA(cudaStreamWaitEvent(g->stream, ready[grp], 0));
+    if (expand4) {
+      Expand4Launch E = *expand4;
+      E.c0 = c0;
+      E.nch = c1 - c0;
+      ProfScope ps(g, RAWSPEC_GB300_K_EXPAND4);
+      RSG_CUDA(expand4_launch(E, g->stream));
+      g->launches++;
+    }
+    for (unsigned i = 0; i < ctx->No; i++)
+      if (launch_product(ctx, g, (int)i, mode[i], inverse, c0, c1)) return 1;
+  }
+  for (unsigned i = 0; i < ctx->No; i++) {
+    Product& P = g->prod[i];
+    if (g->inbuf_count % P.Nis != 0) continue;
+    if (ctx->incoherently_sum) {
+      IcsLaunch I;
+      I.pwr = P.d_out;
+      I.ics = P.d_ics;
+      I.w = g->d_aws;
+      I.Nd = (int)P.Nd;
+      I.np = P.np;
+      I.Nc = (int)ctx->Nc;
+      I.Nant = (int)ctx->Nant;
+      I.N = P.N;
+      ProfScope ps(g, RAWSPEC_GB300_K_ICS);
+      RSG_CUDA(ics_launch(I, g->stream));
+      g->launches++;
+    }
+    // Host functions are queued only when a callback is installed (a NULL
+    // callback would be a no-op on the callback thread anyway).
+    const bool cb = ctx->dump_callback != nullptr;
+    if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
+    {
+      ProfScope ps(g, RAWSPEC_GB300_K_D2H);
+      RSG_CUDA(cudaMemcpyAsync(ctx->h_pwrbuf[i], P.d_out, P.out_bytes, cudaMemcpyDeviceToHost, g->stream));
+      if (ctx->incoherently_sum)
+        RSG_CUDA(cudaMemcpyAsync(ctx->h_icsbuf[i], P.d_ics, P.ics_bytes, cudaMemcpyDeviceToHost, g->stream));
+    }
+    if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, post_dump_fn, &g->cb[i]));
   }
   return 0;
 }
@@ -489,6 +563,9 @@ int rawspec_initialize(rawspec_context* ctx) {
   } while (0)
 
   CK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+  for (int k = 0; k < kMaxCopyGroups; k++) CK(cudaEventCreateWithFlags(&g->ev_ready[k], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&g->ev_free, cudaEventDisableTiming));
 
   const size_t blk_bytes = (size_t)ctx->Ntpb * ctx->Np * ctx->Nc * 2 * (ctx->Nbps / 8);
   // Host input blocks.  Default (cached) pinned memory: on a Grace host the
@@ -694,6 +771,13 @@ void rawspec_cleanup(rawspec_context* ctx) {
     cudaEventDestroy(p.b);
   }
   for (auto e : g->free_events) cudaEventDestroy(e);
+  if (g->copy_stream) {
+    cudaStreamSynchronize(g->copy_stream);
+    cudaStreamDestroy(g->copy_stream);
+  }
+  for (int k = 0; k < kMaxCopyGroups; k++)
+    if (g->ev_ready[k]) cudaEventDestroy(g->ev_ready[k]);
+  if (g->ev_free) cudaEventDestroy(g->ev_free);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
   ctx->gpu_ctx = nullptr;
@@ -771,49 +855,57 @@ int rawspec_zero_blocks_to_gpu(rawspec_context* ctx, off_t dst_idx, size_t num_b
 int rawspec_start_processing(rawspec_context* ctx, int fft_dir) {
   GpuCtx* g = G(ctx);
   if (!g) return 1;
-  const int inverse = fft_dir <= 0 ? 1 : 0;
-  g->inbuf_count++;
-  for (unsigned i = 0; i < ctx->No; i++) {
-    Product& P = g->prod[i];
-    const int mode = ((g->inbuf_count - 1) % P.Nis == 0) ? ACC_WRITE : ACC_ADD;
-    if (launch_product(ctx, g, (int)i, mode, inverse)) return 1;
-    if (g->inbuf_count % P.Nis == 0) {
-      if (ctx->incoherently_sum) {
-        IcsLaunch I;
-        I.pwr = P.d_out;
-        I.ics = P.d_ics;
-        I.w = g->d_aws;
-        I.Nd = (int)P.Nd;
-        I.np = P.np;
-        I.Nc = (int)ctx->Nc;
-        I.Nant = (int)ctx->Nant;
-        I.N = P.N;
-        ProfScope ps(g, RAWSPEC_GB300_K_ICS);
-        RSG_CUDA(ics_launch(I, g->stream));
-        g->launches++;
-      }
-      // Host functions are queued only when a callback is installed (a NULL
-      // callback would be a no-op on the callback thread anyway).
-      const bool cb = ctx->dump_callback != nullptr;
-      if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
-      {
-        ProfScope ps(g, RAWSPEC_GB300_K_D2H);
-        RSG_CUDA(cudaMemcpyAsync(ctx->h_pwrbuf[i], P.d_out, P.out_bytes, cudaMemcpyDeviceToHost, g->stream));
-        if (ctx->incoherently_sum)
-          RSG_CUDA(cudaMemcpyAsync(ctx->h_icsbuf[i], P.d_ics, P.ics_bytes, cudaMemcpyDeviceToHost, g->stream));
-      }
-      if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, post_dump_fn, &g->cb[i]));
-    }
-  }
-  return 0;
+  return process_buffer(ctx, g, fft_dir, 1, nullptr, nullptr);
 }
 
+// The copy of a full buffer is split into channel groups on a copy stream;
+// the kernels of group k start as soon as its copy has landed, so the
+// host-to-device transfer overlaps the processing.  The call returns, like
+// the reference's, once the host blocks may be reused.
 int rawspec_copy_blocks_to_gpu_and_start_processing(rawspec_context* ctx, size_t num_blocks, char expand4bps_to8bps,
                                                     int fft_dir) {
-  int rc = expand4bps_to8bps ? rawspec_copy_blocks_to_gpu_expanding_complex4(ctx, 0, 0, num_blocks)
-                             : rawspec_copy_blocks_to_gpu(ctx, 0, 0, num_blocks);
-  if (rc) return rc;
-  return rawspec_start_processing(ctx, fft_dir);
+  GpuCtx* g = G(ctx);
+  if (!g) return 1;
+  const int ngroups = std::min<int>(kMaxCopyGroups, (int)ctx->Nc);
+  if (num_blocks != ctx->Nb || ngroups < 2 || g->in_bytes < kMinPipelinedBytes) {
+    const int rc = expand4bps_to8bps ? rawspec_copy_blocks_to_gpu_expanding_complex4(ctx, 0, 0, num_blocks)
+                                     : rawspec_copy_blocks_to_gpu(ctx, 0, 0, num_blocks);
+    if (rc) return rc;
+    return rawspec_start_processing(ctx, fft_dir);
+  }
+  const bool packed = expand4bps_to8bps != 0;
+  if (packed && !g->d_in4) {
+    g->in4_bytes = g->in_bytes / 2;
+    if (dev_alloc(g, &g->d_in4, g->in4_bytes)) return 1;
+  }
+  // bytes per channel per block in the host block and in the device buffer
+  const size_t row = packed ? (size_t)ctx->Ntpb * ctx->Np : (size_t)ctx->Ntpb * ctx->Np * 2 * (ctx->Nbps / 8);
+  char* dev = packed ? reinterpret_cast<char*>(g->d_in4) : reinterpret_cast<char*>(g->d_in);
+  // The previous buffer's processing must be finished with the input.
+  RSG_CUDA(cudaEventRecord(g->ev_free, g->stream));
+  RSG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->ev_free, 0));
+  for (int grp = 0; grp < ngroups; grp++) {
+    const size_t c0 = (size_t)grp * ctx->Nc / ngroups;
+    const size_t c1 = (size_t)(grp + 1) * ctx->Nc / ngroups;
+    for (size_t b = 0; b < num_blocks; b++) {
+      RSG_CUDA(cudaMemcpy2DAsync(dev + c0 * ctx->Nb * row + b * row, ctx->Nb * row, ctx->h_blkbufs[b] + c0 * row, row,
+                                 row, c1 - c0, cudaMemcpyHostToDevice, g->copy_stream));
+    }
+    RSG_CUDA(cudaEventRecord(g->ev_ready[grp], g->copy_stream));
+  }
+  Expand4Launch E;
+  if (packed) {
+    E.packed = g->d_in4;
+    E.out = reinterpret_cast<int8_t*>(g->d_in);
+    E.Nc = (int)ctx->Nc;
+    E.Nb = (int)ctx->Nb;
+    E.blk_bytes_packed = (long long)row;
+    E.dst_block = 0;
+    E.num_blocks = (int)num_blocks;
+  }
+  if (process_buffer(ctx, g, fft_dir, ngroups, g->ev_ready, packed ? &E : nullptr)) return 1;
+  RSG_CUDA(cudaStreamSynchronize(g->copy_stream));
+  return 0;
 }
 
 int rawspec_reset_integration(rawspec_context* ctx) {

@@ -237,3 +237,28 @@ def test_unpack_matches_texture_unit(cuda_device, tmp_path):
     assert np.array_equal(t16.view(np.uint32), o16.view(np.uint32)), np.nonzero(t16 != o16)
     # and the oracle's unpack agrees with both
     assert all(float(o8[i]) == O.snorm(int(np.int8(np.uint8(i))), 8) for i in range(256))
+
+
+@pytest.mark.parametrize("nbits", [8, 4])
+def test_combined_call_pipelines_copy_and_processing(cuda_device, nbits):
+    # rawspec_copy_blocks_to_gpu_and_start_processing on buffers of 16 MiB
+    # and more copies channel groups on a second stream and processes each
+    # group as it lands; results must equal the separate calls' and the
+    # oracle's.
+    Nc, Ntpb, nblocks = 8, 1 << 19, 3
+    prods = [(1024, 16, 1), (1 << 16, 1, 4), (8, 128, -4)]
+    if nbits == 4:
+        blocks, _ = synth.int4_blocks(nblocks, Nc, Ntpb, 2, Nant=1, seed=41)
+    else:
+        blocks = synth.gaussian_blocks(nblocks, Nc, Ntpb, 2, sigma=20.0, seed=41)
+    spec = api.Spectrometer(Nc, 2, Ntpb, nbits, prods, conj=1)
+    try:
+        spec.process(blocks, combined=True)
+        got = [np.array(d) for d in spec.dumps]
+    finally:
+        spec.close()
+    c = dict(Nc=Nc, Np=2, Ntpb=Ntpb, nbits=nbits, products=prods, conj=1, fft_dir=1)
+    ref, _ = oracle_for(c, blocks)
+    for i, (nt, na, npol) in enumerate(prods):
+        assert got[i].shape == ref[i].shape
+        assert normalized_error(got[i], ref[i], npol, Nc, nt) < REL_TOL, (nbits, nt)
