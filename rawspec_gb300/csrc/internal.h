@@ -47,12 +47,15 @@ struct SmallLaunch {
   float scale = 1.0f;         // SNORM scale squared, applied to the results
   int vec16 = 0;              // spectra start on 16-byte boundaries (set by small_configure)
   int unit0 = 0, unit_count = 0;  // units of this launch (a channel range; all by default)
+  // split of a unit for launches over a channel group (the pipelined path),
+  // which see 1/pipe_groups of the units and need more CTAs per unit
+  int chunks_pipe = 1, spc_pipe = 0;
 };
 
 // Chooses block size, units per block and chunks per unit.  target_ctas is
 // the number of CTAs that fills the GPU.  Returns 0, or -1 if N is out of
 // range.  partial_floats receives the scratch the launch needs (0 if none).
-int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats);
+int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats, int pipe_groups = 1);
 cudaError_t small_launch(const SmallLaunch& L, cudaStream_t s);
 // Raises the kernel's dynamic shared-memory limit on the current device.
 cudaError_t small_prepare(const SmallLaunch& L);

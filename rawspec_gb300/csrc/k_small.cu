@@ -274,7 +274,7 @@ cudaError_t launch_fmt(const SmallLaunch& L, cudaStream_t s, bool prep) {
 
 int small_radix(int logN, int pol) { return small_info_dyn(logN, 2, pol).R; }
 
-int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats) {
+int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats, int pipe_groups) {
   if (L.logN < 0 || L.logN > 12 || L.M < 1 || L.n_units < 1) return -1;
   const SmallInfo si = small_info_dyn(L.logN, L.nv, L.pol);
   L.tpb = si.TPB;
@@ -293,7 +293,17 @@ int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats) {
   L.spc = (L.M + chunks - 1) / chunks;
   L.chunks = (L.M + L.spc - 1) / L.spc;
   L.grid = ublocks * L.chunks;
-  *partial_floats = L.chunks > 1 ? (size_t)L.n_units * L.chunks * np * ((size_t)1 << L.logN) : 0;
+  // the same for a launch over 1/pipe_groups of the units
+  {
+    const int gunits = std::max(1, L.n_units / std::max(1, pipe_groups));
+    const int gublocks = (gunits + L.sets - 1) / L.sets;
+    int c2 = (target_ctas + gublocks - 1) / gublocks;
+    c2 = std::max(1, std::min(c2, max_chunks));
+    L.spc_pipe = (L.M + c2 - 1) / c2;
+    L.chunks_pipe = (L.M + L.spc_pipe - 1) / L.spc_pipe;
+  }
+  const int cmax = std::max(L.chunks, L.chunks_pipe);
+  *partial_floats = cmax > 1 ? (size_t)L.n_units * cmax * np * ((size_t)1 << L.logN) : 0;
   L.unit0 = 0;
   L.unit_count = L.n_units;
   const long long wbytes = (L.fmt == FMT_I16 ? 4 : 2) * L.nv;

@@ -390,6 +390,10 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
     L.inverse = inverse;
     L.unit0 = c0 * L.units_per_chan;
     L.unit_count = (c1 - c0) * L.units_per_chan;
+    if (c1 - c0 < (int)ctx->Nc) {  // a channel group: the finer split
+      L.chunks = L.chunks_pipe;
+      L.spc = L.spc_pipe;
+    }
     {
       ProfScope ps(g, RAWSPEC_GB300_K_SMALL);
       RSG_CUDA(small_launch(L, g->stream));
@@ -647,7 +651,7 @@ int rawspec_initialize(rawspec_context* ctx) {
       L.out = P.d_out;
       L.conj = ctx->input_conjugated ? 1 : 0;
       size_t pf = 0;
-      if (small_configure(L, target_ctas, &pf)) {
+      if (small_configure(L, target_ctas, &pf, std::min<int>(kMaxCopyGroups, (int)ctx->Nc))) {
         fprintf(stderr, "unsupported FFT length %d\n", P.N);
         FAIL();
       }
