@@ -124,6 +124,7 @@ cudaError_t large_prepare(const LargeLaunch& L);
 bool large_fused_supported(const LargeLaunch& L);
 int large_fused_ring();
 int large_fused_row_radix(int pol);  // radix of the row tiles (twiddle table of twN1)
+int large_fused_col_radix();         // radix of the column tiles (tables twN2 and twM)
 int large_fused_ctl_ints(const LargeLaunch& L);
 cudaError_t large_fused_prepare(LargeLaunch& L);
 cudaError_t large_fused_launch(const LargeLaunch& L, cudaStream_t s);

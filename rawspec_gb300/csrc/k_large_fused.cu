@@ -48,10 +48,18 @@ static_assert(kRingSlots > kLag, "a slot must be released by row tiles queued be
 constexpr int kTilesPerItem = RSG_FUSED_K;  // tiles per work item (amortises the item overheads)
 constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
 
-// Row tiles hold no multi-spectrum accumulators (one spectrum per unit), so
-// all modes run at radix 16.
+// Radices (values per thread per transform).  Row tiles hold no
+// multi-spectrum accumulators (one spectrum per unit); the cross-pol modes
+// keep X0 while X1 is transformed, so they stay at 16.
+#ifndef RSG_FUSED_RA
+#define RSG_FUSED_RA 16
+#endif
+#ifndef RSG_FUSED_RB_TP
+#define RSG_FUSED_RB_TP 16
+#endif
+__host__ __device__ constexpr int fused_ra() { return RSG_FUSED_RA; }
 template <int POL>
-__host__ __device__ constexpr int fused_rb() { return 16; }
+__host__ __device__ constexpr int fused_rb() { return POL == POL_TP ? RSG_FUSED_RB_TP : 16; }
 
 // Resident CTAs per SM the register budget is set for: the polarisations are
 // transformed one after the other (16 complex values per thread), which
@@ -76,7 +84,7 @@ __host__ __device__ constexpr int group_stride(int N, int NV, int C) {
 
 template <int N1, int N2, int NV, int POL>
 struct FusedCfg {
-  static constexpr int RA = 16, TA = N2 / RA, CA = kFusedTPB / TA;
+  static constexpr int RA = fused_ra(), TA = N2 / RA, CA = kFusedTPB / TA;
   static constexpr int RB = fused_rb<POL>(), TB = N1 / RB, CB = kFusedTPB / TB;
   static constexpr int TWA = stockham_tw_size(N2, RA), TWB = stockham_tw_size(N1, RB);
   static constexpr int TWA2 = (TWA + 1) & ~1, TWB2 = (TWB + 1) & ~1;
@@ -435,6 +443,8 @@ bool large_fused_supported(const LargeLaunch& L) {
 int large_fused_ring() { return kRingSlots; }
 
 int large_fused_row_radix(int pol) { return pol == POL_TP ? fused_rb<POL_TP>() : fused_rb<POL_FULL>(); }
+
+int large_fused_col_radix() { return fused_ra(); }
 
 int large_fused_ctl_ints(const LargeLaunch& L) { return 2 + 2 * L.Nc * L.Nss; }
 

@@ -697,7 +697,7 @@ int rawspec_initialize(rawspec_context* ctx) {
       scratch_need = std::max(scratch_need, sf);
       partial_need = std::max(partial_need, pf);
       const int n1 = 1 << L.logN1, n2 = 1 << L.logN2;
-      const int RA = large_pass_a_radix();
+      const int RA = P.fused ? large_fused_col_radix() : large_pass_a_radix();
       const int RB = P.fused ? large_fused_row_radix(pol) : large_pass_b_radix(pol);
       const size_t ta = (size_t)stockham_table_size(n2, RA), tb = (size_t)stockham_table_size(n1, RB);
       const size_t nlo = (size_t)1 << L.h, nhi = (size_t)1 << (L.logN - L.h), nm = (size_t)RA * n1;
