@@ -66,6 +66,10 @@ struct Product {
   int chunks = 1;
   bool fused = false;      // persistent fused four-step kernel
   int* d_ctl = nullptr;    // its control words
+  float* d_partial = nullptr;  // per-chunk partial sums of this product
+  float2* d_scratch = nullptr; // four-step intermediate (or the fused kernel's ring)
+  cudaStream_t stream = nullptr;  // the product's kernels run concurrently with the others'
+  cudaEvent_t ev_join = nullptr;  // end of the product's work for a buffer
 };
 
 struct DumpCb {
@@ -85,16 +89,13 @@ struct GpuCtx {
   cudaStream_t copy_stream = nullptr;     // host-to-device copies of the pipelined path
   cudaEvent_t ev_ready[8] = {nullptr};    // per channel group: its copy has landed
   cudaEvent_t ev_free = nullptr;          // the previous buffer no longer needs the input
+  cudaEvent_t ev_fork = nullptr;          // start of a buffer's work on the product streams
   void* d_in = nullptr;
   size_t in_bytes = 0;
   uint8_t* d_in4 = nullptr;
   size_t in4_bytes = 0;
   int fmt = FMT_I8;
   float* d_aws = nullptr;
-  float* d_partial = nullptr;
-  size_t partial_floats = 0;
-  float2* d_scratch = nullptr;
-  size_t scratch_f2 = 0;
   Product prod[MAX_OUTPUTS];
   unsigned inbuf_count = 0;
   bool caller_managed = false;
@@ -129,18 +130,19 @@ cudaEvent_t take_event(GpuCtx* g) {
 struct ProfScope {
   GpuCtx* g;
   int cls;
+  cudaStream_t st;
   cudaEvent_t a = nullptr;
-  ProfScope(GpuCtx* g_, int cls_) : g(g_), cls(cls_) {
+  ProfScope(GpuCtx* g_, int cls_, cudaStream_t st_ = nullptr) : g(g_), cls(cls_), st(st_ ? st_ : g_->stream) {
     if (g->profiling) {
       a = take_event(g);
-      if (a) cudaEventRecord(a, g->stream);
+      if (a) cudaEventRecord(a, st);
     }
   }
   ~ProfScope() {
     if (g->profiling && a) {
       cudaEvent_t b = take_event(g);
       if (b) {
-        cudaEventRecord(b, g->stream);
+        cudaEventRecord(b, st);
         g->pending.push_back({cls, a, b});
       } else {
         g->free_events.push_back(a);
@@ -363,7 +365,7 @@ int dev_alloc(GpuCtx* g, T** p, size_t bytes) {
 int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int unit0, int n_units, int chunks, int upc,
                     int mode, int inverse, float scale) {
   FinalizeLaunch F;
-  F.partial = g->d_partial;
+  F.partial = P.d_partial;
   F.out = P.d_out;
   F.unit0 = unit0;
   F.n_units = n_units;
@@ -375,8 +377,8 @@ int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int unit0
   F.mode = mode;
   F.inverse = inverse;
   F.scale = scale;
-  ProfScope ps(g, RAWSPEC_GB300_K_FINALIZE);
-  RSG_CUDA(finalize_launch(F, g->stream));
+  ProfScope ps(g, RAWSPEC_GB300_K_FINALIZE, P.stream);
+  RSG_CUDA(finalize_launch(F, P.stream));
   g->launches++;
   return 0;
 }
@@ -395,8 +397,8 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
       L.spc = L.spc_pipe;
     }
     {
-      ProfScope ps(g, RAWSPEC_GB300_K_SMALL);
-      RSG_CUDA(small_launch(L, g->stream));
+      ProfScope ps(g, RAWSPEC_GB300_K_SMALL, P.stream);
+      RSG_CUDA(small_launch(L, P.stream));
       g->launches++;
     }
     if (L.chunks > 1 &&
@@ -411,19 +413,19 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
     L.unit0 = c0 * L.units_per_chan;
     L.unit_count = (c1 - c0) * L.units_per_chan;
     if (P.fused) {
-      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_FUSED);
-      RSG_CUDA(large_fused_launch(L, g->stream));
+      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_FUSED, P.stream);
+      RSG_CUDA(large_fused_launch(L, P.stream));
       g->launches++;
       return 0;
     }
     {
-      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_A);
-      RSG_CUDA(large_launch_a(L, g->stream));
+      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_A, P.stream);
+      RSG_CUDA(large_launch_a(L, P.stream));
       g->launches++;
     }
     {
-      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_B);
-      RSG_CUDA(large_launch_b(L, g->stream));
+      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_B, P.stream);
+      RSG_CUDA(large_launch_b(L, P.stream));
       g->launches++;
     }
     if (L.chunks > 1 &&
@@ -433,14 +435,15 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
   return 0;
 }
 
-// Processes one input buffer: the products' kernels over `ngroups` channel
-// groups (group k waits for ready[k] when given; expand4 expands each
-// group's packed input first), then the dumps of the products whose
-// integration completes.
-int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, const cudaEvent_t* ready,
-                   const Expand4Launch* expand4) {
+// Processes one input buffer: each product's kernels, on the product's own
+// stream, over `ngroups` channel groups (group k waits for ready[k] when
+// given), then the dumps of the products whose integration completes, also
+// on the product's stream; the context stream joins all of them.
+int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, const cudaEvent_t* ready) {
   const int inverse = fft_dir <= 0 ? 1 : 0;
   g->inbuf_count++;
+  RSG_CUDA(cudaEventRecord(g->ev_fork, g->stream));
+  for (unsigned i = 0; i < ctx->No; i++) RSG_CUDA(cudaStreamWaitEvent(g->prod[i].stream, g->ev_fork, 0));
   int mode[MAX_OUTPUTS];
   for (unsigned i = 0; i < ctx->No; i++)
     mode[i] = ((g->inbuf_count - 1) % g->prod[i].Nis == 0) ? ACC_WRITE : ACC_ADD;
@@ -448,46 +451,42 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
     const int c0 = (int)((long long)grp * ctx->Nc / ngroups);
     const int c1 = (int)((long long)(grp + 1) * ctx->Nc / ngroups);
     if (c1 <= c0) continue;
-    if (ready) RSG_CUDA(cudaStreamWaitEvent(g->stream, ready[grp], 0));
-    if (expand4) {
-      Expand4Launch E = *expand4;
-      E.c0 = c0;
-      E.nch = c1 - c0;
-      ProfScope ps(g, RAWSPEC_GB300_K_EXPAND4);
-      RSG_CUDA(expand4_launch(E, g->stream));
-      g->launches++;
-    }
-    for (unsigned i = 0; i < ctx->No; i++)
+    for (unsigned i = 0; i < ctx->No; i++) {
+      if (ready) RSG_CUDA(cudaStreamWaitEvent(g->prod[i].stream, ready[grp], 0));
       if (launch_product(ctx, g, (int)i, mode[i], inverse, c0, c1)) return 1;
+    }
   }
   for (unsigned i = 0; i < ctx->No; i++) {
     Product& P = g->prod[i];
-    if (g->inbuf_count % P.Nis != 0) continue;
-    if (ctx->incoherently_sum) {
-      IcsLaunch I;
-      I.pwr = P.d_out;
-      I.ics = P.d_ics;
-      I.w = g->d_aws;
-      I.Nd = (int)P.Nd;
-      I.np = P.np;
-      I.Nc = (int)ctx->Nc;
-      I.Nant = (int)ctx->Nant;
-      I.N = P.N;
-      ProfScope ps(g, RAWSPEC_GB300_K_ICS);
-      RSG_CUDA(ics_launch(I, g->stream));
-      g->launches++;
+    if (g->inbuf_count % P.Nis == 0) {
+      if (ctx->incoherently_sum) {
+        IcsLaunch I;
+        I.pwr = P.d_out;
+        I.ics = P.d_ics;
+        I.w = g->d_aws;
+        I.Nd = (int)P.Nd;
+        I.np = P.np;
+        I.Nc = (int)ctx->Nc;
+        I.Nant = (int)ctx->Nant;
+        I.N = P.N;
+        ProfScope ps(g, RAWSPEC_GB300_K_ICS, P.stream);
+        RSG_CUDA(ics_launch(I, P.stream));
+        g->launches++;
+      }
+      // Host functions are queued only when a callback is installed (a NULL
+      // callback would be a no-op on the callback thread anyway).
+      const bool cb = ctx->dump_callback != nullptr;
+      if (cb) RSG_CUDA(cudaLaunchHostFunc(P.stream, pre_dump_fn, &g->cb[i]));
+      {
+        ProfScope ps(g, RAWSPEC_GB300_K_D2H, P.stream);
+        RSG_CUDA(cudaMemcpyAsync(ctx->h_pwrbuf[i], P.d_out, P.out_bytes, cudaMemcpyDeviceToHost, P.stream));
+        if (ctx->incoherently_sum)
+          RSG_CUDA(cudaMemcpyAsync(ctx->h_icsbuf[i], P.d_ics, P.ics_bytes, cudaMemcpyDeviceToHost, P.stream));
+      }
+      if (cb) RSG_CUDA(cudaLaunchHostFunc(P.stream, post_dump_fn, &g->cb[i]));
     }
-    // Host functions are queued only when a callback is installed (a NULL
-    // callback would be a no-op on the callback thread anyway).
-    const bool cb = ctx->dump_callback != nullptr;
-    if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
-    {
-      ProfScope ps(g, RAWSPEC_GB300_K_D2H);
-      RSG_CUDA(cudaMemcpyAsync(ctx->h_pwrbuf[i], P.d_out, P.out_bytes, cudaMemcpyDeviceToHost, g->stream));
-      if (ctx->incoherently_sum)
-        RSG_CUDA(cudaMemcpyAsync(ctx->h_icsbuf[i], P.d_ics, P.ics_bytes, cudaMemcpyDeviceToHost, g->stream));
-    }
-    if (cb) RSG_CUDA(cudaLaunchHostFunc(g->stream, post_dump_fn, &g->cb[i]));
+    RSG_CUDA(cudaEventRecord(P.ev_join, P.stream));
+    RSG_CUDA(cudaStreamWaitEvent(g->stream, P.ev_join, 0));
   }
   return 0;
 }
@@ -570,6 +569,11 @@ int rawspec_initialize(rawspec_context* ctx) {
   CK(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
   for (int k = 0; k < kMaxCopyGroups; k++) CK(cudaEventCreateWithFlags(&g->ev_ready[k], cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&g->ev_free, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming));
+  for (int i = 0; i < MAX_OUTPUTS; i++) {
+    CK(cudaStreamCreateWithFlags(&g->prod[i].stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&g->prod[i].ev_join, cudaEventDisableTiming));
+  }
 
   const size_t blk_bytes = (size_t)ctx->Ntpb * ctx->Np * ctx->Nc * 2 * (ctx->Nbps / 8);
   // Host input blocks.  Default (cached) pinned memory: on a Grace host the
@@ -612,7 +616,6 @@ int rawspec_initialize(rawspec_context* ctx) {
   const float snorm_d = ctx->Nbps == 16 ? 32767.0f : 127.0f;
   const float scale = 1.0f / (snorm_d * snorm_d);
   const int target_ctas = g->sm_count * 4;
-  size_t partial_need = 0, scratch_need = 0;
   for (unsigned i = 0; i < ctx->No; i++) {
     Product& P = g->prod[i];
     P.N = (int)ctx->Nts[i];
@@ -655,7 +658,7 @@ int rawspec_initialize(rawspec_context* ctx) {
         fprintf(stderr, "unsupported FFT length %d\n", P.N);
         FAIL();
       }
-      partial_need = std::max(partial_need, pf);
+      if (pf && dev_alloc(g, &P.d_partial, pf * sizeof(float))) FAIL();
       const int R = small_radix(P.logN, pol);
       const size_t ntw = (size_t)std::max(stockham_table_size(P.N, R), 1);
       if (dev_alloc(g, &P.d_tw, ntw * sizeof(float2))) FAIL();
@@ -694,8 +697,8 @@ int rawspec_initialize(rawspec_context* ctx) {
         CK(cudaMemsetAsync(P.d_ctl, 0, nctl * sizeof(int), g->stream));
         L.ctl = P.d_ctl;
       }
-      scratch_need = std::max(scratch_need, sf);
-      partial_need = std::max(partial_need, pf);
+      if (sf && dev_alloc(g, &P.d_scratch, sf * sizeof(float2))) FAIL();
+      if (pf && dev_alloc(g, &P.d_partial, pf * sizeof(float))) FAIL();
       const int n1 = 1 << L.logN1, n2 = 1 << L.logN2;
       const int RA = P.fused ? large_fused_col_radix() : large_pass_a_radix();
       const int RB = P.fused ? large_fused_row_radix(pol) : large_pass_b_radix(pol);
@@ -717,18 +720,10 @@ int rawspec_initialize(rawspec_context* ctx) {
       else CK(large_prepare(L));
     }
   }
-  if (partial_need) {
-    if (dev_alloc(g, &g->d_partial, partial_need * sizeof(float))) FAIL();
-    g->partial_floats = partial_need;
-  }
-  if (scratch_need) {
-    if (dev_alloc(g, &g->d_scratch, scratch_need * sizeof(float2))) FAIL();
-    g->scratch_f2 = scratch_need;
-  }
   for (unsigned i = 0; i < ctx->No; i++) {
-    g->prod[i].sl.partial = g->d_partial;
-    g->prod[i].ll.partial = g->d_partial;
-    g->prod[i].ll.scratch = g->d_scratch;
+    g->prod[i].sl.partial = g->prod[i].d_partial;
+    g->prod[i].ll.partial = g->prod[i].d_partial;
+    g->prod[i].ll.scratch = g->prod[i].d_scratch;
   }
   CK(cudaStreamSynchronize(g->stream));
   g->inbuf_count = 0;
@@ -762,14 +757,20 @@ void rawspec_cleanup(rawspec_context* ctx) {
   cudaFree(g->d_in);
   cudaFree(g->d_in4);
   cudaFree(g->d_aws);
-  cudaFree(g->d_partial);
-  cudaFree(g->d_scratch);
   for (int i = 0; i < MAX_OUTPUTS; i++) {
     cudaFree(g->prod[i].d_out);
     cudaFree(g->prod[i].d_ics);
     cudaFree(g->prod[i].d_tw);
     cudaFree(g->prod[i].d_ctl);
+    cudaFree(g->prod[i].d_partial);
+    cudaFree(g->prod[i].d_scratch);
+    if (g->prod[i].stream) {
+      cudaStreamSynchronize(g->prod[i].stream);
+      cudaStreamDestroy(g->prod[i].stream);
+    }
+    if (g->prod[i].ev_join) cudaEventDestroy(g->prod[i].ev_join);
   }
+  if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   for (auto& p : g->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
@@ -859,7 +860,7 @@ int rawspec_zero_blocks_to_gpu(rawspec_context* ctx, off_t dst_idx, size_t num_b
 int rawspec_start_processing(rawspec_context* ctx, int fft_dir) {
   GpuCtx* g = G(ctx);
   if (!g) return 1;
-  return process_buffer(ctx, g, fft_dir, 1, nullptr, nullptr);
+  return process_buffer(ctx, g, fft_dir, 1, nullptr);
 }
 
 // The copy of a full buffer is split into channel groups on a copy stream;
@@ -895,19 +896,24 @@ int rawspec_copy_blocks_to_gpu_and_start_processing(rawspec_context* ctx, size_t
       RSG_CUDA(cudaMemcpy2DAsync(dev + c0 * ctx->Nb * row + b * row, ctx->Nb * row, ctx->h_blkbufs[b] + c0 * row, row,
                                  row, c1 - c0, cudaMemcpyHostToDevice, g->copy_stream));
     }
+    if (packed) {  // the group's 4-bit samples are expanded right behind its copy
+      Expand4Launch E;
+      E.packed = g->d_in4;
+      E.out = reinterpret_cast<int8_t*>(g->d_in);
+      E.Nc = (int)ctx->Nc;
+      E.Nb = (int)ctx->Nb;
+      E.blk_bytes_packed = (long long)row;
+      E.dst_block = 0;
+      E.num_blocks = (int)num_blocks;
+      E.c0 = (int)c0;
+      E.nch = (int)(c1 - c0);
+      ProfScope ps(g, RAWSPEC_GB300_K_EXPAND4, g->copy_stream);
+      RSG_CUDA(expand4_launch(E, g->copy_stream));
+      g->launches++;
+    }
     RSG_CUDA(cudaEventRecord(g->ev_ready[grp], g->copy_stream));
   }
-  Expand4Launch E;
-  if (packed) {
-    E.packed = g->d_in4;
-    E.out = reinterpret_cast<int8_t*>(g->d_in);
-    E.Nc = (int)ctx->Nc;
-    E.Nb = (int)ctx->Nb;
-    E.blk_bytes_packed = (long long)row;
-    E.dst_block = 0;
-    E.num_blocks = (int)num_blocks;
-  }
-  if (process_buffer(ctx, g, fft_dir, ngroups, g->ev_ready, packed ? &E : nullptr)) return 1;
+  if (process_buffer(ctx, g, fft_dir, ngroups, g->ev_ready)) return 1;
   RSG_CUDA(cudaStreamSynchronize(g->copy_stream));
   return 0;
 }
