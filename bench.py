@@ -25,6 +25,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -122,18 +123,40 @@ def load_traffic() -> dict:
     return {}
 
 
+_CPU_CASES: dict = {}
+
+
 def cpu_sample_run(nthreads: int, nc_sample: int, reps: int = 1) -> tuple[float, float]:
     """Times the OpenMP FP32 CPU chain on nc_sample channels of one buffer of
-    the workload; returns (GB/s of RAW input, seconds)."""
+    the workload, reps times; returns (GB/s of RAW input, seconds per rep)."""
     from oracle import oracle as O
     from rawspec_gb300 import synth
-    blocks = synth.gaussian_blocks(2, nc_sample, NTPB, NP, sigma=SIGMA, seed=1)
-    cfg = O.make_cfg(nc_sample, NP, NTPB, 2, NBITS, products(1))
+    if nc_sample not in _CPU_CASES:
+        blocks = synth.gaussian_blocks(2, nc_sample, NTPB, NP, sigma=SIGMA, seed=1)
+        _CPU_CASES[nc_sample] = (blocks, O.make_cfg(nc_sample, NP, NTPB, 2, NBITS, products(1)))
+    blocks, cfg = _CPU_CASES[nc_sample]
     t0 = time.perf_counter()
     for _ in range(reps):
         O.run_cpu(cfg, blocks, nthreads=nthreads)
     dt = (time.perf_counter() - t0) / reps
     return blocks.nbytes / dt / 1e9, dt
+
+
+def cpu_baseline_leg(min_seconds: float = 12.0) -> dict:
+    """The CPU chain on whole buffers of the workload (all 64 channels),
+    repeated until at least min_seconds of CPU work have been timed."""
+    from oracle import oracle as O
+    threads = O.lib().cpu_max_threads()
+    cpu_sample_run(threads, NC)  # warm-up (page-in, thread pool)
+    reps, secs = 0, 0.0
+    while secs < min_seconds:
+        _, dt = cpu_sample_run(threads, NC)
+        secs += dt
+        reps += 1
+    v = reps * 2 * BLOCK_BYTES / secs / 1e9
+    return {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"{reps} whole buffers (64 channels x 2 blocks, 256 MiB RAW each), all three products, "
+                      f"total power, {secs:.1f} s"}
 
 
 def run_reference(args, rank, world):
@@ -142,7 +165,9 @@ def run_reference(args, rank, world):
         return 0
     from oracle import oracle as O
     threads = O.lib().cpu_max_threads()
-    nc_sample = max(8, threads)
+    # one step = one whole buffer (64 channels x 2 blocks, about 0.5 s on 16
+    # host cores), so the default --steps/--warmup run takes well under a minute
+    nc_sample = NC
     for _ in range(args.warmup):
         cpu_sample_run(threads, nc_sample)
     vals, secs = [], 0.0
@@ -151,7 +176,7 @@ def run_reference(args, rank, world):
         vals.append(v)
         secs += dt
     value = statistics.median(vals)
-    sample = f"{nc_sample} of 64 channels x 1 buffer (2 blocks) per step, all three products, total power"
+    sample = "one whole buffer per step (64 channels x 2 blocks, 256 MiB RAW), all three products, total power"
     line = {
         "metric": "RAW-in GB/s", "value": value, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
@@ -202,8 +227,6 @@ def run_native(args, rank, world, local_rank):
         for _ in range(args.warmup):
             spec.start()
         spec.wait()
-        spec.reset_profile()
-        spec.set_profiling(True)
         l0 = spec.kernel_launches()
         sampler = ClockSampler(local_rank)
         sampler.start()
@@ -223,6 +246,19 @@ def run_native(args, rank, world, local_rank):
         launches = spec.kernel_launches() - l0
         ms = max_over_ranks(e0.elapsed_time(e1))
         spec.wait()
+        # per-kernel device times: a separate pass in which the library runs
+        # the products one after another, so each kernel's events time it alone
+        spec.reset_profile()
+        spec.set_profiling(True)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(args.steps):
+            if lib.rawspec_start_processing(cp, 1) != 0:
+                raise RuntimeError("start_processing failed")
+        p1.record(stream)
+        p1.synchronize()
+        ms_serial = p0.elapsed_time(p1)
         prof = {}
         for k, name in enumerate(api.KERNEL_CLASS_NAMES):
             t, n = spec.profile(k)
@@ -251,7 +287,7 @@ def run_native(args, rank, world, local_rank):
         for i in range(3):
             n_dumps = (start + args.steps) // nis[i] - start // nis[i]
             d2h += n_dumps * sizes[i]
-        results[npol] = dict(ms=ms, prof=prof, launches=launches, clocks=clocks, e2e_s=e2e_s,
+        results[npol] = dict(ms=ms, ms_serial=ms_serial, prof=prof, launches=launches, clocks=clocks, e2e_s=e2e_s,
                              d2h=d2h / args.steps, device_bytes=int(lib.rawspec_gb300_device_bytes(cp)))
         spec.close()
 
@@ -287,6 +323,17 @@ def run_native(args, rank, world, local_rank):
         t_ms, n = prof[dom]
         traffic = tr.get(dom_name)
     achieved = alg / (t_ms / max(n, 1) / 1e3) / 1e9 if n else None
+    # FP32 view of the same kernel: 5 N log2 N flops per complex transform
+    # plus 4 per detected sample (total power), against the nominal non-tensor
+    # FP32 rate of 152 SMs x 128 lanes x 2 flops x 2.07 GHz
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    if dom in ("large_a", "large_b", "large_fused"):
+        nt_dom = [PRODUCTS[0][0]]
+    else:
+        nt_dom = [PRODUCTS[1][0], PRODUCTS[2][0]]
+    samples = NC * NP * 2 * NTPB  # complex samples of one buffer, both polarisations
+    flops = sum(samples * (5 * math.log2(nt) + 4) for nt in nt_dom) / len(nt_dom)
+    fp32_tflops = flops / (t_ms / max(n, 1) / 1e3) / 1e12 if n else None
     line = {
         "metric": "RAW-in GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -301,20 +348,19 @@ def run_native(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_source": peak_src,
-                     "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()}},
+                     "fp32": {"achieved_tflops": fp32_tflops, "peak_tflops": fp32_peak, "peak_source": "nominal",
+                              "frac": (fp32_tflops / fp32_peak) if fp32_tflops else None},
+                     "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
+                     "kernel_timing": "CUDA events around each launch in a separate pass with the products "
+                                      "serialised on one stream",
+                     "serialised_ms_per_step": r["ms_serial"] / args.steps},
         "npolout4": {"value": world * step_bytes * args.steps / (results[4]["ms"] / 1e3) / 1e9,
                      "e2e": world * step_bytes * args.steps / results[4]["e2e_s"] / 1e9,
                      "ms_per_step": results[4]["ms"] / args.steps},
         "device_bytes": r["device_bytes"],
     }
     if rank == 0 and world == 1 and not args.no_cpu:
-        from oracle import oracle as O
-        threads = O.lib().cpu_max_threads()
-        nc_sample = max(8, threads)
-        v, dt = cpu_sample_run(threads, nc_sample)
-        line["cpu_baseline"] = {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
-                                "sample": f"{nc_sample} of 64 channels x 1 buffer, all three products, "
-                                          f"total power, {dt:.1f} s"}
+        line["cpu_baseline"] = cpu_baseline_leg()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

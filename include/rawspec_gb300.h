@@ -38,14 +38,18 @@ int rawspec_gb300_product_info(const rawspec_context *ctx, int product,
                                unsigned int *Nss, unsigned int *Nis,
                                unsigned int *Nd);
 
-/* The CUDA stream (cudaStream_t) all work of the context is queued on. */
+/* The context's CUDA stream (cudaStream_t).  Every call's work is ordered on
+ * it: the products' kernels run on per-product streams that fork from it and
+ * join back into it, so an event recorded on it brackets a whole buffer. */
 void *rawspec_gb300_stream(rawspec_context *ctx);
 
 /* Device pointer and size of the device input buffer
  * ([channel][Nb*Ntpb][pol][re,im] bytes). */
 void *rawspec_gb300_device_input(rawspec_context *ctx, size_t *bytes);
 
-/* Enables (1) or disables (0) per-kernel CUDA-event timing. */
+/* Enables (1) or disables (0) per-kernel CUDA-event timing.  While enabled,
+ * the products run one after another on the context stream, so that each
+ * kernel's events time it alone on the GPU. */
 int rawspec_gb300_set_profiling(rawspec_context *ctx, int enable);
 
 /* Waits for the stream, then returns the accumulated device time (ms) and

@@ -68,7 +68,9 @@ struct Product {
   int* d_ctl = nullptr;    // its control words
   float* d_partial = nullptr;  // per-chunk partial sums of this product
   float2* d_scratch = nullptr; // four-step intermediate (or the fused kernel's ring)
-  cudaStream_t stream = nullptr;  // the product's kernels run concurrently with the others'
+  cudaStream_t own_stream = nullptr;  // the product's kernels run concurrently with the others'
+  cudaStream_t stream = nullptr;      // stream of the current buffer (own_stream, or the context
+                                      // stream while profiling serialises the products)
   cudaEvent_t ev_join = nullptr;  // end of the product's work for a buffer
 };
 
@@ -443,7 +445,11 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
   const int inverse = fft_dir <= 0 ? 1 : 0;
   g->inbuf_count++;
   RSG_CUDA(cudaEventRecord(g->ev_fork, g->stream));
-  for (unsigned i = 0; i < ctx->No; i++) RSG_CUDA(cudaStreamWaitEvent(g->prod[i].stream, g->ev_fork, 0));
+  for (unsigned i = 0; i < ctx->No; i++) {
+    Product& P = g->prod[i];
+    P.stream = g->profiling ? g->stream : P.own_stream;
+    RSG_CUDA(cudaStreamWaitEvent(P.stream, g->ev_fork, 0));
+  }
   int mode[MAX_OUTPUTS];
   for (unsigned i = 0; i < ctx->No; i++)
     mode[i] = ((g->inbuf_count - 1) % g->prod[i].Nis == 0) ? ACC_WRITE : ACC_ADD;
@@ -571,7 +577,8 @@ int rawspec_initialize(rawspec_context* ctx) {
   CK(cudaEventCreateWithFlags(&g->ev_free, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming));
   for (int i = 0; i < MAX_OUTPUTS; i++) {
-    CK(cudaStreamCreateWithFlags(&g->prod[i].stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&g->prod[i].own_stream, cudaStreamNonBlocking));
+    g->prod[i].stream = g->prod[i].own_stream;
     CK(cudaEventCreateWithFlags(&g->prod[i].ev_join, cudaEventDisableTiming));
   }
 
@@ -764,9 +771,9 @@ void rawspec_cleanup(rawspec_context* ctx) {
     cudaFree(g->prod[i].d_ctl);
     cudaFree(g->prod[i].d_partial);
     cudaFree(g->prod[i].d_scratch);
-    if (g->prod[i].stream) {
-      cudaStreamSynchronize(g->prod[i].stream);
-      cudaStreamDestroy(g->prod[i].stream);
+    if (g->prod[i].own_stream) {
+      cudaStreamSynchronize(g->prod[i].own_stream);
+      cudaStreamDestroy(g->prod[i].own_stream);
     }
     if (g->prod[i].ev_join) cudaEventDestroy(g->prod[i].ev_join);
   }
