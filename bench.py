@@ -53,6 +53,46 @@ def rank_info():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+class RankGroup:
+    """Host-side coordination of the replicas of a multi-GPU run: one process
+    per GPU, each with its own context and its own data (the channels of
+    different ranks are independent, so no data moves between ranks).  Only
+    the barrier around the timed region and the max over ranks of the timings
+    go through the process group (gloo, on the host)."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max_over_ranks(self, x: float) -> float:
+        if self.dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def whole_job_gbs(world: int, step_bytes: int, steps: int, seconds_max: float) -> float:
+    """Whole-job RAW-in GB/s: every rank processes steps x step_bytes; the
+    job takes as long as its slowest rank."""
+    return world * step_bytes * steps / seconds_max / 1e9
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -197,22 +237,8 @@ def run_native(args, rank, world, local_rank):
     from rawspec_gb300 import api, synth
 
     torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist_mod
-        dist_mod.init_process_group("gloo")
-        dist = dist_mod
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    group = RankGroup(world)
+    barrier, max_over_ranks = group.barrier, group.max_over_ranks
 
     blocks = synth.gaussian_blocks(2, NC, NTPB, NP, sigma=SIGMA, seed=1 + rank)
     results = {}
@@ -293,8 +319,8 @@ def run_native(args, rank, world, local_rank):
 
     r = results[1]
     step_bytes = 2 * BLOCK_BYTES
-    value = world * step_bytes * args.steps / (r["ms"] / 1e3) / 1e9
-    e2e = world * step_bytes * args.steps / r["e2e_s"] / 1e9
+    value = whole_job_gbs(world, step_bytes, args.steps, r["ms"] / 1e3)
+    e2e = whole_job_gbs(world, step_bytes, args.steps, r["e2e_s"])
     # dominant kernel class of the headline run
     prof = r["prof"]
     kernel_classes = ["small", "finalize", "large_a", "large_b", "ics", "expand4", "large_fused"]
@@ -354,8 +380,8 @@ def run_native(args, rank, world, local_rank):
                      "kernel_timing": "CUDA events around each launch in a separate pass with the products "
                                       "serialised on one stream",
                      "serialised_ms_per_step": r["ms_serial"] / args.steps},
-        "npolout4": {"value": world * step_bytes * args.steps / (results[4]["ms"] / 1e3) / 1e9,
-                     "e2e": world * step_bytes * args.steps / results[4]["e2e_s"] / 1e9,
+        "npolout4": {"value": whole_job_gbs(world, step_bytes, args.steps, results[4]["ms"] / 1e3),
+                     "e2e": whole_job_gbs(world, step_bytes, args.steps, results[4]["e2e_s"]),
                      "ms_per_step": results[4]["ms"] / args.steps},
         "device_bytes": r["device_bytes"],
     }
@@ -363,8 +389,7 @@ def run_native(args, rank, world, local_rank):
         line["cpu_baseline"] = cpu_baseline_leg()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    group.close()
     return 0
 
 
