@@ -2,9 +2,11 @@
 // and the kernel translation units.  Plain C++ types only.
 #pragma once
 
+#include <cuda.h>
+#include <cuda_runtime.h>
+
 #include <cstddef>
 #include <cstdint>
-#include <cuda_runtime.h>
 
 namespace rsg {
 
@@ -104,6 +106,10 @@ struct LargeLaunch {
   int ring = 0;                   // intermediate slots
   int* ctl = nullptr;             // [0] error, [1] item counter, [2..2+S) A done, [2+S..2+2S) B done
   int fused_ctas = 0;             // persistent grid size
+  // fused kernel: tensor maps of the input (rows of N1 words), of the
+  // twiddle tables twJ and twM and of the dump buffer (rows of N2 floats)
+  const float2* twJ = nullptr;    // [j][n1] = W_N^(n1*j), j < N2 / R_A
+  CUtensorMap tmap_in, tmap_twj, tmap_twm, tmap_out;
 };
 int large_configure(LargeLaunch& L, int target_ctas, size_t* scratch_float2, size_t* partial_floats);
 // Radix of pass A (values per thread of its N2-point FFT) and its threads per
@@ -117,8 +123,9 @@ cudaError_t large_launch_a(const LargeLaunch& L, cudaStream_t s);
 cudaError_t large_launch_b(const LargeLaunch& L, cudaStream_t s);
 // Raises both kernels' dynamic shared-memory limits on the current device.
 cudaError_t large_prepare(const LargeLaunch& L);
-// Persistent fused variant (k_large_fused.cu): supported for 8-bit input,
-// 2^16 <= N <= 2^22 and integration units of one spectrum; needs a ring of
+// Persistent fused variant (k_large_fused.cu): supported for 8-bit input of
+// two polarisations, 2^16 <= N <= 2^22 and integration units of one
+// spectrum; needs a ring of
 // large_fused_ring() intermediate slabs and large_fused_ctl_ints() control
 // words (zeroed once before the first launch).
 bool large_fused_supported(const LargeLaunch& L);
@@ -126,6 +133,7 @@ int large_fused_ring();
 int large_fused_row_radix(int pol);  // radix of the row tiles (twiddle table of twN1)
 int large_fused_col_radix();         // radix of the column tiles (tables twN2 and twM)
 int large_fused_ctl_ints(const LargeLaunch& L);
+int large_fused_twj_entries(const LargeLaunch& L);  // size of the twJ table
 cudaError_t large_fused_prepare(LargeLaunch& L);
 cudaError_t large_fused_launch(const LargeLaunch& L, cudaStream_t s);
 

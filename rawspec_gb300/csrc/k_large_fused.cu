@@ -15,9 +15,23 @@
 // B(s-RING) tile has released the slot.  An item only ever waits for items
 // earlier in the order, which were taken by CTAs that are running, so the
 // waits always end; they are bounded nonetheless and record an error instead
-// of hanging if the bound is ever reached.  Column and row tiles of
-// neighbouring slabs run side by side on the SMs, so the loads of one overlap
-// the arithmetic of another, and the intermediate rarely leaves L2.
+// of hanging if the bound is ever reached.
+//
+// Data movement.  Every tile's input reaches shared memory through the
+// copy engine of the SM (TMA), double-buffered: the column tiles' 8-bit
+// words as a 2-D tensor copy ([N2 rows] x [C_A words], rows N1 words apart),
+// the row tiles' intermediate rows as 1-D bulk copies, one stage per
+// polarisation.  A stage's buffer becomes the transform's exchange buffer
+// once its values are in registers, and the next stage is requested as soon
+// as the transform is done with it; the first two stages of the CTA's next
+// work item are requested while the current one finishes (the item is taken
+// one ahead), so the loads of one item overlap the arithmetic of the other.
+// Completion is tracked by two mbarriers (expected-transaction counts).
+// Intermediate rows are discarded from L2 once copied (they are dead), so
+// the ring is never written back to HBM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 
 #include "detect.cuh"
@@ -46,52 +60,67 @@ static_assert(kRingSlots > kLag, "a slot must be released by row tiles queued be
 #define RSG_FUSED_K 2
 #endif
 constexpr int kTilesPerItem = RSG_FUSED_K;  // tiles per work item (amortises the item overheads)
-constexpr long long kSpinLimit = 1ll << 24;  // ~2 s of polling at most
+static_assert(kTilesPerItem >= 2, "an item must fill both stage buffers");
+#ifndef RSG_FUSED_DISCARD
+#define RSG_FUSED_DISCARD 1
+#endif
+constexpr long long kSpinLimit = 1ll << 24;         // polls of a counter (~2 s with back-off)
+constexpr long long kMbarCycles = 4000000000ll;     // ~2 s of SM clocks for a stage copy
 
-// Radices (values per thread per transform).  Row tiles hold no
-// multi-spectrum accumulators (one spectrum per unit); the cross-pol modes
-// keep X0 while X1 is transformed, so they stay at 16.
+// Radix (values per thread per transform) of the column and row tiles.
 #ifndef RSG_FUSED_RA
 #define RSG_FUSED_RA 16
 #endif
 #ifndef RSG_FUSED_RB_TP
 #define RSG_FUSED_RB_TP 16
 #endif
+#ifndef RSG_FUSED_RB_X
+#define RSG_FUSED_RB_X 16
+#endif
 __host__ __device__ constexpr int fused_ra() { return RSG_FUSED_RA; }
 template <int POL>
-__host__ __device__ constexpr int fused_rb() { return POL == POL_TP ? RSG_FUSED_RB_TP : 16; }
-
-// Resident CTAs per SM the register budget is set for: the polarisations are
-// transformed one after the other (16 complex values per thread), which
-// leaves room for three CTAs in total-power mode; the cross-pol modes keep the
-// first polarisation's spectrum while the second is transformed.
-#ifndef RSG_FUSED_TP_MINB
-#define RSG_FUSED_TP_MINB 2
-#endif
-template <int POL>
-__host__ __device__ constexpr int fused_minb() { return POL == POL_TP ? RSG_FUSED_TP_MINB : 2; }
+__host__ __device__ constexpr int fused_rb() { return POL == POL_TP ? RSG_FUSED_RB_TP : RSG_FUSED_RB_X; }
 
 // Shared-memory distance between the exchange buffers of neighbouring
 // interleaved sub-FFTs, chosen so that the C sub-FFTs served by one
-// half-warp land on disjoint banks.
-__host__ __device__ constexpr int group_stride(int N, int NV, int C) {
-  int base = NV * smem_padded_len(N);
+// half-warp land on disjoint banks, and even (16-byte aligned rows for the
+// bulk copies).
+__host__ __device__ constexpr int group_stride(int N, int C) {
+  int base = smem_padded_len(N);
   const int cp = C < 16 ? C : 16;
   const int want = (16 / cp) % 16;
   while (base % 16 != want) ++base;
-  return base;
+  return base + (base & 1);
 }
 
-template <int N1, int N2, int NV, int POL>
+__host__ __device__ constexpr int round16(int x) { return (x + 15) & ~15; }
+
+template <int N1, int N2, int POL>
 struct FusedCfg {
   static constexpr int RA = fused_ra(), TA = N2 / RA, CA = kFusedTPB / TA;
   static constexpr int RB = fused_rb<POL>(), TB = N1 / RB, CB = kFusedTPB / TB;
   static constexpr int TWA = stockham_tw_size(N2, RA), TWB = stockham_tw_size(N1, RB);
-  static constexpr int TWA2 = (TWA + 1) & ~1, TWB2 = (TWB + 1) & ~1;
-  static constexpr int GSA = group_stride(N2, 1, CA), GSB = group_stride(N1, 1, CB);
-  static constexpr int XCH = CA * GSA > CB * GSB ? CA * GSA : CB * GSB;
-  static constexpr size_t SMEM = (size_t)(TWA2 + TWB2 + XCH) * sizeof(float2);
+  static constexpr int GSA = group_stride(N2, CA), GSB = group_stride(N1, CB);
+  // column-tile words: boxes of BOXR rows x CW words (CW >= 4: 16-byte rows)
+  static constexpr int CW = CA < 4 ? 4 : CA;
+  static constexpr int BOXR = N2 < 256 ? N2 : 256;
+  // row-tile outputs through tensor stores: total power (one plane) with rows
+  // of at least 16 bytes; boxes of BOXO spectrum rows x C_B bins
+  static constexpr bool TMA_OUT = POL == POL_TP && CB >= 4;
+  static constexpr int BOXO = N1 / 2 < 256 ? N1 / 2 : 256;
+  static constexpr int XCH = round16(CA * GSA > CB * GSB ? CA * GSA : CB * GSB);  // float2 per stage buffer
+  static constexpr int TWS = round16((TA + RA) * CA);   // float2: column-tile twiddle slices per stage
+  static constexpr int OUTS = TMA_OUT ? round16(CB * N1 / 2) : 0;  // float2: staged row-tile outputs
+  static constexpr int OFF_TWB = round16(TWA), OFF_STG = OFF_TWB + round16(TWB);
+  static constexpr int OFF_TWS = OFF_STG + 2 * XCH, OFF_OUT = OFF_TWS + 2 * TWS;
+  static constexpr size_t SMEM = (size_t)(OFF_OUT + OUTS) * sizeof(float2) + 128;  // + alignment slack
+  static constexpr unsigned BYTES_A = (unsigned)N2 * CW * 4;
+  static constexpr unsigned BYTES_TW = (unsigned)(TA + RA) * CA * 8;
+  static constexpr unsigned BYTES_B = (unsigned)CB * N1 * 8;
   static_assert(TA * CA == kFusedTPB && TB * CB == kFusedTPB, "sub-FFT threads must tile the CTA");
+  static_assert((size_t)BYTES_A <= (size_t)XCH * sizeof(float2), "column words must fit a stage buffer");
+  static_assert(N2 % BOXR == 0 && CA % 2 == 0, "tensor boxes must tile the column");
+  static_assert(N1 % (2 * BOXO) == 0, "output boxes must not straddle the FFT shift");
 };
 
 struct Sync {
@@ -147,25 +176,9 @@ __device__ __forceinline__ unsigned long long policy_evict_last() {
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
   return p;
 }
-__device__ __forceinline__ uint32_t ld_u32_hint(const uint32_t* p, unsigned long long pol) {
-  uint32_t v;
-  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ uint16_t ld_u16_hint(const uint16_t* p, unsigned long long pol) {
-  uint16_t v;
-  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
-  return v;
-}
 __device__ __forceinline__ void st_f2_hint(float2* p, float2 v, unsigned long long pol) {
   asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
                : "memory");
-}
-__device__ __forceinline__ float2 ld_f2_hint(const float2* p, unsigned long long pol) {
-  float2 v;
-  asm volatile("ld.global.cg.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol)
-               : "memory");
-  return v;
 }
 __device__ __forceinline__ float ld_f_hint(const float* p, unsigned long long pol) {
   float v;
@@ -175,43 +188,148 @@ __device__ __forceinline__ float ld_f_hint(const float* p, unsigned long long po
 __device__ __forceinline__ void st_f_hint(float* p, float v, unsigned long long pol) {
   asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
 }
-template <typename W>
-struct HintLoad;
-template <>
-struct HintLoad<uint32_t> {
-  static __device__ __forceinline__ uint32_t ld(const uint32_t* p, unsigned long long pol) { return ld_u32_hint(p, pol); }
+
+// ---- mbarrier and bulk-copy primitives (PTX ISA: mbarrier, cp.async.bulk) ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* mb, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mb)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* mb, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mb)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* mb, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(mb)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase of the given parity to complete (bounded by SM clock
+// cycles; on time-out the error word is set and the CTA carries on).
+__device__ __forceinline__ void mbar_wait(unsigned long long* mb, unsigned parity, int* err) {
+  if (mbar_try_wait(mb, parity)) return;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(mb, parity)) {
+    if (clock64() - t0 > kMbarCycles) {
+      atomicExch(err, 3);
+      return;
+    }
+  }
+}
+// Orders this CTA's earlier generic-proxy accesses of shared memory before
+// later asynchronous-proxy (copy engine) writes to it.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* mb,
+                                            unsigned long long policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_addr(mb)), "l"(policy)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* mb) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(mb))
+               : "memory");
+}
+// Tensor stores from shared memory: plain (first buffer of an integration)
+// or reduce-add into the accumulator (later buffers); one bulk group per tile.
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<unsigned long long>(map)),
+               "r"(x), "r"(y), "r"(smem_addr(src))
+               : "memory");
+}
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<unsigned long long>(map)),
+               "r"(x), "r"(y), "r"(smem_addr(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// The bulk groups committed so far have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// The bulk groups committed so far are complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// The 128-byte L2 line at p holds dead data: drop it without writing it back.
+__device__ __forceinline__ void discard_l2(const void* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
+
+// A work item: K consecutive column tiles (A) or row tiles (B) of one slab.
+// Segment k of the order holds A(k) (k < S) followed by B(k - lag) (k >= lag).
+struct Item {
+  bool isA;
+  int slab, titem;
 };
-template <>
-struct HintLoad<uint16_t> {
-  static __device__ __forceinline__ uint16_t ld(const uint16_t* p, unsigned long long pol) { return ld_u16_hint(p, pol); }
-};
+__device__ __forceinline__ Item decode_item(long long item, int S, int itemsA, int itemsB) {
+  Item it;
+  const int p1 = S < kLag ? S : kLag;       // A-only segments
+  const int mid = S > kLag ? S - kLag : 0;  // A+B segments
+  const long long n1 = (long long)p1 * itemsA;
+  const long long n2 = (long long)mid * (itemsA + itemsB);
+  if (item < n1) {
+    it.isA = true;
+    it.slab = (int)(item / itemsA);
+    it.titem = (int)(item % itemsA);
+  } else if (item < n1 + n2) {
+    const long long i2 = item - n1;
+    const int k = kLag + (int)(i2 / (itemsA + itemsB));
+    const int r = (int)(i2 % (itemsA + itemsB));
+    it.isA = r < itemsA;
+    it.slab = it.isA ? k : k - kLag;
+    it.titem = it.isA ? r : r - itemsA;
+  } else {  // B-only tail
+    const long long i3 = item - n1 - n2;
+    it.isA = false;
+    it.slab = mid + (int)(i3 / itemsB);
+    it.titem = (int)(i3 % itemsB);
+  }
+  return it;
+}
 
 }  // namespace
 
-template <int N1, int N2, int FMT, int NV, int POL>
-__global__ void __launch_bounds__(kFusedTPB, fused_minb<POL>())
-k_large_fused(LargeLaunch a) {
-  using F = FusedCfg<N1, N2, NV, POL>;
+// TOUT: row-tile outputs through tensor stores (total power, forward
+// transforms, F::TMA_OUT); otherwise per-thread stores (and loads of the
+// accumulator in accumulate mode).
+template <int N1, int N2, int POL, bool TOUT>
+__global__ void __launch_bounds__(kFusedTPB, 2)
+k_large_fused(const __grid_constant__ LargeLaunch a) {
+  using F = FusedCfg<N1, N2, POL>;
+  static_assert(!TOUT || F::TMA_OUT, "tensor-store outputs need one plane and 16-byte rows");
   constexpr int N = N1 * N2;
   constexpr int NP = PolOut<POL>::NP;
+  constexpr int K = kTilesPerItem;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* twA = reinterpret_cast<float2*>(smem_raw);
-  float2* twB = twA + F::TWA2;
-  float2* xch = twB + F::TWB2;
-  __shared__ long long s_item;
+  float2* twA = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  float2* twB = twA + F::OFF_TWB;
+  float2* stg = twA + F::OFF_STG;  // two stage buffers of F::XCH float2
+  float2* tws = twA + F::OFF_TWS;  // two twiddle-slice buffers of F::TWS float2
+  float* outs = reinterpret_cast<float*>(twA + F::OFF_OUT);  // [N1 shifted rows][C_B bins]
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ long long s_next;
+  __shared__ int s_pre;
 
   const int tid = threadIdx.x;
-  for (int i = tid; i < F::TWA; i += kFusedTPB) twA[i] = a.twN2[i];
-  for (int i = tid; i < F::TWB; i += kFusedTPB) twB[i] = a.twN1[i];
-  __syncthreads();
-
   const int S = a.S;
   constexpr int tilesA = N1 / F::CA, tilesB = N2 / F::CB;
-  constexpr int K = kTilesPerItem;
   static_assert(tilesA % K == 0 && tilesB % K == 0, "items must cover whole tiles");
   constexpr int itemsA = tilesA / K, itemsB = tilesB / K;
   const long long total = (long long)S * (itemsA + itemsB);
-  int* err = a.ctl;       // sticky error word (never reset by a launch)
+  int* err = a.ctl;  // sticky error word (never reset by a launch)
   int* next = a.ctl + 1;
   int* doneA = a.ctl + 2;
   int* doneB = a.ctl + 2 + S;
@@ -219,120 +337,188 @@ k_large_fused(LargeLaunch a) {
   const unsigned long long pol_first = policy_evict_first();
   const unsigned long long pol_last = policy_evict_last();
 
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_init_fence();
+    s_next = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
+    s_pre = 0;
+  }
+  for (int i = tid; i < F::TWA; i += kFusedTPB) twA[i] = a.twN2[i];
+  for (int i = tid; i < F::TWB; i += kFusedTPB) twB[i] = a.twN1[i];
+  __syncthreads();
+
+  // Stage copies (issued by thread 0).  Column stage t of an item: the C_A
+  // columns of tile titem*K + t, all N2 rows, as 8-bit words, plus the
+  // tile's twiddle slices; row stage s: polarisation s%2 of the C_B rows of
+  // tile titem*K + s/2, from the ring.
+  auto issue_stage = [&](const Item& it, int s, int buf) {
+    float2* dst = stg + (size_t)buf * F::XCH;
+    unsigned long long* mb = &mbar[buf];
+    if (it.isA) {
+      const int tile = it.titem * K + s;
+      const long long gs = (long long)a.slab0 + it.slab;
+      const long long row0 = ((gs / a.Nss) * a.chan_stride + (gs % a.Nss) * (long long)N) / N1;
+      const int x0 = (tile * F::CA) & ~3;  // 16-byte aligned start column
+      mbar_expect_tx(mb, F::BYTES_A + F::BYTES_TW);
+      uint32_t* words = reinterpret_cast<uint32_t*>(dst);
+#pragma unroll 1
+      for (int i = 0; i < N2 / F::BOXR; ++i)
+        tma_load_2d(words + (size_t)i * F::BOXR * F::CW, &a.tmap_in, x0, (int)(row0 + (long long)i * F::BOXR), mb,
+                    pol_first);
+      float2* tw = tws + (size_t)buf * F::TWS;
+      tma_load_2d(tw, &a.tmap_twj, tile * F::CA, 0, mb, pol_last);
+      tma_load_2d(tw + F::TA * F::CA, &a.tmap_twm, tile * F::CA, 0, mb, pol_last);
+    } else {
+      const int tile = it.titem * K + (s >> 1);
+      const int q = s & 1;
+      const float2* src =
+          a.scratch + (size_t)(it.slab % a.ring) * 2 * N + ((size_t)q * N2 + (size_t)tile * F::CB) * N1;
+      mbar_expect_tx(mb, F::BYTES_B);
+#pragma unroll 1
+      for (int r = 0; r < F::CB; ++r) bulk_load(dst + (size_t)r * F::GSB, src + (size_t)r * N1, N1 * 8, mb);
+    }
+  };
+
+  unsigned ph = 0;  // bit b: parity of the next completion of stage buffer b
+  bool pre_ok = false;  // thread 0: the next item's first stages are in flight
   for (;;) {
-    if (tid == 0) s_item = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
-    __syncthreads();
-    const long long item = s_item;
+    __syncthreads();  // the previous item's s_next / s_pre are written
+    const long long item = s_next;
+    const int pre = s_pre;
     __syncthreads();
     if (item >= total) break;
-
-    // Decode the item.  Segment k holds A(k) (k < S) followed by B(k - lag)
-    // (k >= lag); each item covers K consecutive tiles of one slab.
-    bool isA;
-    int slab, titem;
-    {
-      const int p1 = S < kLag ? S : kLag;                 // A-only segments
-      const int mid = S > kLag ? S - kLag : 0;            // A+B segments
-      const long long n1 = (long long)p1 * itemsA;
-      const long long n2 = (long long)mid * (itemsA + itemsB);
-      if (item < n1) {
-        isA = true;
-        slab = (int)(item / itemsA);
-        titem = (int)(item % itemsA);
-      } else if (item < n1 + n2) {
-        const long long i2 = item - n1;
-        const int k = kLag + (int)(i2 / (itemsA + itemsB));
-        const int r = (int)(i2 % (itemsA + itemsB));
-        isA = r < itemsA;
-        slab = isA ? k : k - kLag;
-        titem = isA ? r : r - itemsA;
-      } else {                                            // B-only tail
-        const long long i3 = item - n1 - n2;
-        isA = false;
-        slab = mid + (int)(i3 / itemsB);
-        titem = (int)(i3 % itemsB);
-      }
+    const Item it = decode_item(item, S, itemsA, itemsB);
+    long long nxt = 0;
+    if (tid == 0) {
+      nxt = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
+      s_next = nxt;
+      pre_ok = false;
     }
-    const int slot = slab % a.ring;
-    float2* scr = a.scratch + (size_t)slot * NV * N;
+    const int nstages = it.isA ? K : 2 * K;
+    // Requests stage s + 2 into the buffer stage s has released: the item's
+    // own, else the next item's first stages (B only once its column tiles
+    // are all published).  Called by every thread after a CTA barrier that
+    // follows the last use of the buffer.
+    auto refill = [&](int s) {
+      if (tid != 0) return;
+      const int buf = s & 1;
+      if (s + 2 < nstages) {
+        fence_proxy_async();
+        issue_stage(it, s + 2, buf);
+        return;
+      }
+      if (nxt >= total) return;
+      const Item nit = decode_item(nxt, S, itemsA, itemsB);
+      if (s + 2 == nstages) pre_ok = nit.isA || load_acquire(doneA + nit.slab) >= tilesA;
+      if (pre_ok) {
+        fence_proxy_async();
+        issue_stage(nit, s + 2 - nstages, buf);
+      }
+    };
 
-    if (isA) {
-      if (slab >= a.ring) wait_count(doneB + (slab - a.ring), tilesB, err, 1);
+    const int slot = it.slab % a.ring;
+    float2* scr = a.scratch + (size_t)slot * 2 * N;
+
+    if (it.isA) {
+      if (tid == 0 && !pre) {
+        fence_proxy_async();
+        issue_stage(it, 0, 0);
+        issue_stage(it, 1, 1);
+      }
+      if (it.slab >= a.ring) wait_count(doneB + (it.slab - a.ring), tilesB, err, 1);
       // ---- K column tiles: N2-point FFTs of C_A columns n1 each ------------
       constexpr int R = F::RA, T = F::TA, C = F::CA;
       const int col = tid % C;
       const int j = tid / C;
-      const int c = (a.slab0 + slab) / a.Nss;
-      const int sp = (a.slab0 + slab) % a.Nss;
-      using W = typename SampleWord<FMT, NV>::type;
-      const W* src0 = reinterpret_cast<const W*>(a.in) + (long long)c * a.chan_stride + (long long)sp * N + col +
-                      (long long)N1 * j;
-      W w[R];
-      {
-        const W* src = src0 + titem * K * C;
-#pragma unroll
-        for (int m = 0; m < R; ++m) w[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
-      }
 #pragma unroll 1
       for (int t = 0; t < K; ++t) {
-        const int n1 = (titem * K + t) * C + col;
-        W wn[R];  // next tile's samples, requested before this tile's FFTs
-        if (t + 1 < K) {
-          const W* src = src0 + (titem * K + t + 1) * C;
+        const int buf = t & 1;
+        float2* sb = stg + (size_t)buf * F::XCH;
+        const float2* tw = tws + (size_t)buf * F::TWS;  // [T][C] then [R][C]
+        mbar_wait(&mbar[buf], (ph >> buf) & 1u, err);
+        ph ^= 1u << buf;
+        const int tile = it.titem * K + t;
+        const int n1 = tile * C + col;
+        uint32_t w[R];
+        {
+          const uint32_t* words = reinterpret_cast<const uint32_t*>(sb) + ((tile * C) & 3) + col;
 #pragma unroll
-          for (int m = 0; m < R; ++m) wn[m] = HintLoad<W>::ld(src + (long long)N1 * T * m, pol_first);
+          for (int m = 0; m < R; ++m) w[m] = words[(j + T * m) * F::CW];
         }
-        const int e0 = n1 * j;
-        const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
+        __syncthreads();  // the buffer becomes the exchange buffer; tile t-1 is done
+        if (t > 0) refill(t - 1);
+        const float2 w0 = tw[j * C + col];  // W_N^(n1 j)
         float2* dst = scr + n1;
-        const float2* twm = a.twM + n1;
 #pragma unroll
-        for (int q = 0; q < NV; ++q) {
+        for (int q = 0; q < 2; ++q) {
           float2 v[1][R];
 #pragma unroll
           for (int m = 0; m < R; ++m) {
-            float2 smp[NV];
-            Unpack<FMT, NV>::run(w[m], smp);
-            v[0][m] = q == 0 ? smp[0] : smp[NV - 1];
+            float2 smp[2];
+            Unpack<FMT_I8, 2>::run(w[m], smp);
+            v[0][m] = smp[q];
           }
-          GroupFFT<N2, R, 1>::run(v, j, xch + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
+          GroupFFT<N2, R, 1>::run(v, j, sb + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
 #pragma unroll
           for (int m = 0; m < R; ++m) {
             const int k2 = j + m * T;
-            const float2 tw = m == 0 ? w0 : cmul(w0, __ldg(twm + (size_t)m * N1));
-            st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[0][m], tw), pol_last);
+            // W_N^(n1 k2) = W_N^(n1 j) W_N^(n1 m T)
+            const float2 twk = m == 0 ? w0 : cmul(w0, tw[(T + m) * C + col]);
+            st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[0][m], twk), pol_last);
           }
         }
-        if (t + 1 < K) {
-#pragma unroll
-          for (int m = 0; m < R; ++m) w[m] = wn[m];
+      }
+      publish(doneA + it.slab, K);
+      refill(K - 1);
+    } else {
+      if (!pre) {
+        wait_count(doneA + it.slab, tilesA, err, 2);
+        if (tid == 0) {
+          fence_proxy_async();
+          issue_stage(it, 0, 0);
+          issue_stage(it, 1, 1);
         }
       }
-      publish(doneA + slab, K);
-    } else {
-      wait_count(doneA + slab, tilesA, err, 2);
       // ---- K row tiles: N1-point FFTs of C_B rows k2, detection, store ----
       constexpr int R = F::RB, T = F::TB, C = F::CB;
       const int row = tid % C;
       const int j = tid / C;
-      const int c = (a.slab0 + slab) / a.units_per_chan;
-      const int d = (a.slab0 + slab) % a.units_per_chan;
+      const int c = (a.slab0 + it.slab) / a.units_per_chan;
+      const int d = (a.slab0 + it.slab) % a.units_per_chan;
       float* obase = a.out + ((size_t)d * NP * a.Nc + c) * N;
       const size_t plane = (size_t)a.Nc * N;
 #pragma unroll 1
       for (int t = 0; t < K; ++t) {
-        const int k2 = (titem * K + t) * C + row;
-        const float2* src = scr + (size_t)k2 * N1 + j;
+        const int tile = it.titem * K + t;
+        const int k2 = tile * C + row;
         // Polarisation 0, then 1; total power accumulates |X|^2 of each, the
         // cross-pol modes keep X0 while X1 is transformed.
-        float2 x0[NV == 2 && POL != POL_TP ? R : 1];
+        float2 x0[POL != POL_TP ? R : 1];
         float tp[POL == POL_TP ? R : 1];
         float2 v[1][R];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) {
+        for (int q = 0; q < 2; ++q) {
+          const int s = 2 * t + q;
+          const int buf = s & 1;
+          float2* sb = stg + (size_t)buf * F::XCH;
+          mbar_wait(&mbar[buf], (ph >> buf) & 1u, err);
+          ph ^= 1u << buf;
 #pragma unroll
-          for (int m = 0; m < R; ++m) v[0][m] = ld_f2_hint(src + (size_t)q * N2 * N1 + m * T, pol_first);
-          GroupFFT<N1, R, 1>::run(v, j, xch + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
+          for (int m = 0; m < R; ++m) v[0][m] = sb[(size_t)row * F::GSB + j + m * T];
+#if RSG_FUSED_DISCARD
+          {
+            const char* rows = reinterpret_cast<const char*>(scr + ((size_t)q * N2 + (size_t)tile * C) * N1);
+            constexpr int kLines = F::BYTES_B / 128;
+#pragma unroll 1
+            for (int l = tid; l < kLines; l += kFusedTPB) discard_l2(rows + (size_t)l * 128);
+          }
+#endif
+          // the previous tile's output copy must have read the staging area
+          if (TOUT && q == 0 && tid == 0) bulk_wait_read();
+          __syncthreads();  // the buffer becomes the exchange buffer
+          GroupFFT<N1, R, 1>::run(v, j, sb + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
+          refill(s);
           if constexpr (POL == POL_TP) {
 #pragma unroll
             for (int m = 0; m < R; ++m) {
@@ -347,6 +533,30 @@ k_large_fused(LargeLaunch a) {
               for (int m = 0; m < R; ++m) x0[m] = v[0][m];
             }
           }
+        }
+        if constexpr (TOUT) {
+          // Shifted bin k2 + N2*((k1 + N1/2) mod N1): staged as
+          // [row (k1 + N1/2) mod N1][k2 - tile*C], then written (first
+          // buffer) or added (later buffers) by tensor copies.
+#pragma unroll
+          for (int m = 0; m < R; ++m) {
+            const int k1s = (j + m * T + N1 / 2) & (N1 - 1);
+            outs[k1s * C + row] = tp[m] * a.scale;
+          }
+          fence_proxy_async();
+          __syncthreads();
+          if (tid == 0) {
+            const int y0 = (int)(((long long)d * NP * a.Nc + c) * N1);
+#pragma unroll 1
+            for (int i = 0; i < N1 / F::BOXO; ++i) {
+              if (a.mode == ACC_ADD)
+                tma_reduce_add_2d(&a.tmap_out, tile * C, y0 + i * F::BOXO, outs + i * F::BOXO * C);
+              else
+                tma_store_2d(&a.tmap_out, tile * C, y0 + i * F::BOXO, outs + i * F::BOXO * C);
+            }
+            bulk_commit();
+          }
+          continue;
         }
         // Detection and store, MC bins at a time: in accumulate mode the
         // MC*NP old values are all requested before the first store.
@@ -383,9 +593,12 @@ k_large_fused(LargeLaunch a) {
           }
         }
       }
-      publish(doneB + slab, K);
+      publish(doneB + it.slab, K);
     }
+    if (tid == 0) s_pre = pre_ok ? 1 : 0;
   }
+  // output copies still in flight complete before the CTA retires
+  if (TOUT && tid == 0) bulk_wait_all();
 }
 
 // ---------------------------------------------------------------------------
@@ -393,11 +606,17 @@ k_large_fused(LargeLaunch a) {
 // ---------------------------------------------------------------------------
 namespace {
 
-template <int N1, int N2, int NV, int POL>
+template <int N1, int N2, int POL>
 cudaError_t fused_t(const LargeLaunch& L, cudaStream_t s, int mode_op, int* ctas_out) {
-  using F = FusedCfg<N1, N2, NV, POL>;
-  auto k = k_large_fused<N1, N2, FMT_I8, NV, POL>;
-  if (mode_op == 1) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F::SMEM);
+  using F = FusedCfg<N1, N2, POL>;
+  auto k = (F::TMA_OUT && !L.inverse) ? k_large_fused<N1, N2, POL, F::TMA_OUT> : k_large_fused<N1, N2, POL, false>;
+  if (mode_op == 1) {
+    cudaError_t e = cudaFuncSetAttribute(k_large_fused<N1, N2, POL, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F::SMEM);
+    if (e != cudaSuccess || !F::TMA_OUT) return e;
+    return cudaFuncSetAttribute(k_large_fused<N1, N2, POL, F::TMA_OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)F::SMEM);
+  }
   if (mode_op == 2) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
@@ -407,17 +626,27 @@ cudaError_t fused_t(const LargeLaunch& L, cudaStream_t s, int mode_op, int* ctas
     *ctas_out = std::max(1, per_sm) * sms;
     return cudaSuccess;
   }
+  if (mode_op == 3) {  // tensor-map geometry
+    ctas_out[0] = F::CW;
+    ctas_out[1] = F::BOXR;
+    ctas_out[2] = F::CA;
+    ctas_out[3] = F::TA;
+    ctas_out[4] = F::RA;
+    ctas_out[5] = F::CB;
+    ctas_out[6] = F::BOXO;
+    ctas_out[7] = F::TMA_OUT ? 1 : 0;
+    return cudaSuccess;
+  }
   k<<<L.fused_ctas, kFusedTPB, F::SMEM, s>>>(L);
   return cudaGetLastError();
 }
 
 template <int N1, int N2>
 cudaError_t fused_pol(const LargeLaunch& L, cudaStream_t s, int op, int* ctas) {
-  if (L.nv == 1) return fused_t<N1, N2, 1, POL_TP>(L, s, op, ctas);
   switch (L.pol) {
-    case POL_FULL: return fused_t<N1, N2, 2, POL_FULL>(L, s, op, ctas);
-    case POL_STOKES: return fused_t<N1, N2, 2, POL_STOKES>(L, s, op, ctas);
-    default: return fused_t<N1, N2, 2, POL_TP>(L, s, op, ctas);
+    case POL_FULL: return fused_t<N1, N2, POL_FULL>(L, s, op, ctas);
+    case POL_STOKES: return fused_t<N1, N2, POL_STOKES>(L, s, op, ctas);
+    default: return fused_t<N1, N2, POL_TP>(L, s, op, ctas);
   }
 }
 
@@ -434,10 +663,27 @@ cudaError_t fused_dispatch(const LargeLaunch& L, cudaStream_t s, int op, int* ct
   }
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
 }  // namespace
 
 bool large_fused_supported(const LargeLaunch& L) {
-  return L.fmt == FMT_I8 && L.M == 1 && L.logN >= 16 && L.logN <= 22 && L.logN2 == (L.logN + 1) / 2;
+  if (L.fmt != FMT_I8 || L.nv != 2 || L.M != 1 || L.logN < 16 || L.logN > 22) return false;
+  if (L.logN2 != (L.logN + 1) / 2) return false;
+  const long long n1 = 1ll << L.logN1;
+  // the column tiles' tensor copies view each channel as rows of N1 words
+  return L.chan_stride % n1 == 0 && (reinterpret_cast<uintptr_t>(L.in) & 15) == 0;
 }
 
 int large_fused_ring() { return kRingSlots; }
@@ -448,10 +694,57 @@ int large_fused_col_radix() { return fused_ra(); }
 
 int large_fused_ctl_ints(const LargeLaunch& L) { return 2 + 2 * L.Nc * L.Nss; }
 
+namespace {
+
+// 2-D tensor map: rows of `width` elements of `esize` bytes, `pitch` bytes apart.
+cudaError_t encode_2d(CUtensorMap* map, const void* base, CUtensorMapDataType type, int esize,
+                      unsigned long long width, unsigned long long rows, unsigned long long pitch, int box_w,
+                      int box_h) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return cudaErrorNotSupported;
+  (void)esize;
+  cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch};
+  cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, type, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+int large_fused_twj_entries(const LargeLaunch& L) {
+  return (1 << L.logN1) * ((1 << L.logN2) / fused_ra());
+}
+
 cudaError_t large_fused_prepare(LargeLaunch& L) {
   cudaError_t e = fused_dispatch(L, nullptr, 1, nullptr);
   if (e != cudaSuccess) return e;
-  return fused_dispatch(L, nullptr, 2, &L.fused_ctas);
+  e = fused_dispatch(L, nullptr, 2, &L.fused_ctas);
+  if (e != cudaSuccess) return e;
+  int geo[8] = {0};
+  e = fused_dispatch(L, nullptr, 3, geo);
+  if (e != cudaSuccess) return e;
+  const int CW = geo[0], BOXR = geo[1], CA = geo[2], TA = geo[3], RA = geo[4], CB = geo[5], BOXO = geo[6];
+  const unsigned long long n1 = 1ull << L.logN1, n2 = 1ull << L.logN2;
+  // the input buffer as rows of N1 32-bit words (one word: a sample of both
+  // polarisations)
+  e = encode_2d(&L.tmap_in, L.in, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, n1, (unsigned long long)L.Nc * L.chan_stride / n1,
+                n1 * 4, CW, BOXR);
+  if (e != cudaSuccess) return e;
+  // twiddle tables [T_A][N1] (W_N^(n1 j)) and [R_A][N1] (W_N^(n1 m T_A)), 8-byte entries
+  e = encode_2d(&L.tmap_twj, L.twJ, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, n1, (unsigned long long)TA, n1 * 8, CA, TA);
+  if (e != cudaSuccess) return e;
+  e = encode_2d(&L.tmap_twm, L.twM, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, n1, (unsigned long long)RA, n1 * 8, CA, RA);
+  if (e != cudaSuccess) return e;
+  // the dump buffer [units][|P|][Nc][N] as rows of N2 floats (total power)
+  if (geo[7]) {
+    const unsigned long long rows = (unsigned long long)L.units_per_chan * L.Nc * n1;
+    e = encode_2d(&L.tmap_out, L.out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, n2, rows, n2 * 4, CB, BOXO);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t large_fused_launch(const LargeLaunch& L, cudaStream_t s) {

@@ -709,20 +709,28 @@ int rawspec_initialize(rawspec_context* ctx) {
       const int n1 = 1 << L.logN1, n2 = 1 << L.logN2;
       const int RA = P.fused ? large_fused_col_radix() : large_pass_a_radix();
       const int RB = P.fused ? large_fused_row_radix(pol) : large_pass_b_radix(pol);
+      // tables at 256-byte aligned offsets (the fused kernel copies twM and
+      // twJ with the tensor copy engine)
+      auto al = [](size_t n) { return (n + 31) & ~size_t(31); };
       const size_t ta = (size_t)stockham_table_size(n2, RA), tb = (size_t)stockham_table_size(n1, RB);
       const size_t nlo = (size_t)1 << L.h, nhi = (size_t)1 << (L.logN - L.h), nm = (size_t)RA * n1;
-      if (dev_alloc(g, &P.d_tw, (ta + tb + nlo + nhi + nm) * sizeof(float2))) FAIL();
+      const size_t nj = P.fused ? (size_t)large_fused_twj_entries(L) : 0;
+      const size_t o_tb = al(ta), o_lo = o_tb + al(tb), o_hi = o_lo + al(nlo), o_m = o_hi + al(nhi);
+      const size_t o_j = o_m + al(nm);
+      if (dev_alloc(g, &P.d_tw, (o_j + nj) * sizeof(float2))) FAIL();
       L.twN2 = P.d_tw;
-      L.twN1 = P.d_tw + ta;
-      L.twLo = P.d_tw + ta + tb;
-      L.twHi = P.d_tw + ta + tb + nlo;
-      L.twM = P.d_tw + ta + tb + nlo + nhi;
+      L.twN1 = P.d_tw + o_tb;
+      L.twLo = P.d_tw + o_lo;
+      L.twHi = P.d_tw + o_hi;
+      L.twM = P.d_tw + o_m;
+      L.twJ = P.fused ? P.d_tw + o_j : nullptr;
       L.scale = scale;
       CK(stockham_twiddle_fill(P.d_tw, n2, RA, g->stream));
-      CK(stockham_twiddle_fill(P.d_tw + ta, n1, RB, g->stream));
-      CK(twiddle_fill(P.d_tw + ta + tb, (long long)nlo, (long long)P.N, 1, g->stream));
-      CK(twiddle_fill(P.d_tw + ta + tb + nlo, (long long)nhi, (long long)P.N, (long long)nlo, g->stream));
-      CK(passa_twiddle_fill(P.d_tw + ta + tb + nlo + nhi, n1, RA, (long long)(n2 / RA), (long long)P.N, g->stream));
+      CK(stockham_twiddle_fill(P.d_tw + o_tb, n1, RB, g->stream));
+      CK(twiddle_fill(P.d_tw + o_lo, (long long)nlo, (long long)P.N, 1, g->stream));
+      CK(twiddle_fill(P.d_tw + o_hi, (long long)nhi, (long long)P.N, (long long)nlo, g->stream));
+      CK(passa_twiddle_fill(P.d_tw + o_m, n1, RA, (long long)(n2 / RA), (long long)P.N, g->stream));
+      if (P.fused) CK(passa_twiddle_fill(P.d_tw + o_j, n1, n2 / RA, 1, (long long)P.N, g->stream));
       if (P.fused) CK(large_fused_prepare(L));
       else CK(large_prepare(L));
     }
@@ -955,7 +963,8 @@ int rawspec_wait_for_completion(rawspec_context* ctx) {
     int err = 0;
     if (cudaMemcpy(&err, g->prod[i].d_ctl, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
     if (err) {
-      fprintf(stderr, "rawspec: product %u: a dependency wait of the fused FFT kernel timed out (code %d)\n", i, err);
+      fprintf(stderr, "rawspec: product %u: a bounded wait of the fused FFT kernel timed out (code %d: 1 ring slot, "
+                      "2 column tiles, 3 stage copy)\n", i, err);
       return 1;
     }
   }

@@ -70,15 +70,28 @@ def test_small_lengths_all_modes(cuda_device, logn, npol):
     assert err < REL_TOL, (nt, npol, err)
 
 
-@pytest.mark.parametrize("logn", [13, 14, 16, 18, 20])
-def test_large_lengths(cuda_device, logn):
+@pytest.mark.parametrize("logn,npol", [(13, 4), (14, 1), (16, 4), (17, -4), (18, 1), (19, 4), (20, 4), (21, 1),
+                                       (22, -4)])
+def test_large_lengths(cuda_device, logn, npol):
+    # every four-step shape (N1 x N2 from 64 x 128 to 2048 x 2048), both the
+    # two-kernel and the fused path, integrations spanning two buffers
     nt = 1 << logn
-    c = dict(Nc=1, Np=2, Ntpb=nt // 2, nbits=8, nblocks=4, products=[(nt, 2, 4)], conj=0, fft_dir=1)
+    c = dict(Nc=1, Np=2, Ntpb=nt // 2, nbits=8, nblocks=4, products=[(nt, 2, npol)], conj=0, fft_dir=1)
     blocks = synth.gaussian_blocks(4, 1, nt // 2, 2, sigma=16.0, seed=200 + logn)
     dumps, _, _, _ = run_gpu(c, blocks)
     ref, _ = oracle_for(c, blocks)
-    err = normalized_error(dumps[0], ref[0], 4, 1, nt)
+    err = normalized_error(dumps[0], ref[0], npol, 1, nt)
     assert err < REL_TOL, (nt, err)
+
+
+def test_large_single_polarisation(cuda_device):
+    # one input polarisation takes the two-kernel four-step path
+    nt = 1 << 16
+    c = dict(Nc=2, Np=1, Ntpb=nt, nbits=8, nblocks=2, products=[(nt, 1, 1)], conj=0, fft_dir=1)
+    blocks = synth.gaussian_blocks(2, 2, nt, 1, sigma=16.0, seed=250)
+    dumps, _, _, _ = run_gpu(c, blocks)
+    ref, _ = oracle_for(c, blocks)
+    assert normalized_error(dumps[0], ref[0], 1, 2, nt) < REL_TOL
 
 
 @pytest.mark.parametrize("npol,conj,fft_dir", [(1, 0, 1), (4, 1, -1), (-4, 1, 1)])
