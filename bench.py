@@ -40,6 +40,7 @@ sys.path.insert(0, str(ROOT))
 NC, NP, NTPB, NBITS = 64, 2, 524288, 8
 PRODUCTS = [(1 << 20, 51), (8, 128), (1024, 3072)]
 SIGMA = 20.0
+E2E_REPS = 5
 BLOCK_BYTES = NC * NTPB * NP * 2
 WORKLOAD = "production shape: 64 ch x 2 pol int8, Ntpb 524288 (128 MiB blocks), Nfft 2^20/8/1024, Nint 51/128/3072"
 
@@ -290,30 +291,38 @@ def run_native(args, rank, world, local_rank):
             t, n = spec.profile(k)
             prof[name] = (t, n)
         spec.set_profiling(False)
-        # end-to-end through the C-ABI from pinned host blocks
-        for _ in range(max(1, args.warmup // 2)):
+        # end-to-end through the C-ABI from pinned host blocks: K steps of the
+        # reference CLI's per-buffer sequence (rawspec.c:1012-1014), timed
+        # five times (host jitter moves single runs); the median is reported,
+        # every sample is kept
+        nbuf = args.warmup + 2 * args.steps  # buffers processed so far
+        for _ in range(args.warmup):
             spec.copy_and_start()
             spec.wait()
+            nbuf += 1
         sizes = [spec.ctx.h_pwrbuf_size[i] for i in range(3)]
         nis = [spec.product_info(i)[1] for i in range(3)]
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            # the reference CLI's per-buffer sequence (rawspec.c:1012-1014)
+        reps, d2h = [], 0
+        for _ in range(E2E_REPS):
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                if lib.rawspec_wait_for_completion(cp) != 0:
+                    raise RuntimeError("wait failed")
+                if lib.rawspec_copy_blocks_to_gpu_and_start_processing(cp, 2, 0, 1) != 0:
+                    raise RuntimeError("copy/start failed")
             if lib.rawspec_wait_for_completion(cp) != 0:
                 raise RuntimeError("wait failed")
-            if lib.rawspec_copy_blocks_to_gpu_and_start_processing(cp, 2, 0, 1) != 0:
-                raise RuntimeError("copy/start failed")
-        if lib.rawspec_wait_for_completion(cp) != 0:
-            raise RuntimeError("wait failed")
-        e2e_s = max_over_ranks(time.perf_counter() - t0)
-        # device->host dump bytes per step (dump schedule over the timed steps)
-        start = args.warmup + max(1, args.warmup // 2) + args.steps
-        d2h = 0
-        for i in range(3):
-            n_dumps = (start + args.steps) // nis[i] - start // nis[i]
-            d2h += n_dumps * sizes[i]
+            reps.append(max_over_ranks(time.perf_counter() - t0))
+            # device->host dump bytes of these buffers (a product dumps after
+            # every Nis-th buffer)
+            for b in range(nbuf + 1, nbuf + args.steps + 1):
+                d2h += sum(sizes[i] for i in range(3) if b % nis[i] == 0)
+            nbuf += args.steps
+        e2e_s = statistics.median(reps)
+        d2h /= E2E_REPS
         results[npol] = dict(ms=ms, ms_serial=ms_serial, prof=prof, launches=launches, clocks=clocks, e2e_s=e2e_s,
+                             e2e_samples=[whole_job_gbs(world, 2 * BLOCK_BYTES, args.steps, x) for x in reps],
                              d2h=d2h / args.steps, device_bytes=int(lib.rawspec_gb300_device_bytes(cp)))
         spec.close()
 
@@ -368,7 +377,8 @@ def run_native(args, rank, world, local_rank):
                    "l2": "inputs larger than L2 (256 MiB per step, resident)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": step_bytes,
-                "d2h_bytes_per_step": int(r["d2h"])},
+                "d2h_bytes_per_step": int(r["d2h"]), "samples": r["e2e_samples"],
+                "timing": f"wall clock of K steps, median of {E2E_REPS} runs"},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",

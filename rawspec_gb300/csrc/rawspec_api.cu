@@ -38,7 +38,10 @@ namespace {
 using namespace rsg;
 
 constexpr int kMaxLogN = 24;
-constexpr int kMaxCopyGroups = 8;                     // channel groups of the pipelined copy
+#ifndef RSG_COPY_GROUPS
+#define RSG_COPY_GROUPS 8
+#endif
+constexpr int kMaxCopyGroups = RSG_COPY_GROUPS;       // channel groups of the pipelined copy
 constexpr size_t kMinPipelinedBytes = size_t(16) << 20;  // smaller buffers are copied in one piece
 
 #define RSG_CUDA(call)                                                                   \
@@ -89,7 +92,7 @@ struct GpuCtx {
   int sm_count = 152;
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;     // host-to-device copies of the pipelined path
-  cudaEvent_t ev_ready[8] = {nullptr};    // per channel group: its copy has landed
+  cudaEvent_t ev_ready[kMaxCopyGroups] = {nullptr};  // per channel group: its copy has landed
   cudaEvent_t ev_free = nullptr;          // the previous buffer no longer needs the input
   cudaEvent_t ev_fork = nullptr;          // start of a buffer's work on the product streams
   void* d_in = nullptr;
