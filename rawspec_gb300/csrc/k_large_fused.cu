@@ -180,13 +180,12 @@ __device__ __forceinline__ void st_f2_hint(float2* p, float2 v, unsigned long lo
   asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
                : "memory");
 }
-__device__ __forceinline__ float ld_f_hint(const float* p, unsigned long long pol) {
-  float v;
-  asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol) : "memory");
-  return v;
-}
 __device__ __forceinline__ void st_f_hint(float* p, float v, unsigned long long pol) {
   asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
+}
+// *p += v, performed in L2 without returning a value (no wait on the thread).
+__device__ __forceinline__ void red_add_f_hint(float* p, float v, unsigned long long pol) {
+  asm volatile("red.global.add.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
 }
 
 // ---- mbarrier and bulk-copy primitives (PTX ISA: mbarrier, cp.async.bulk) ----
@@ -558,38 +557,26 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
           }
           continue;
         }
-        // Detection and store, MC bins at a time: in accumulate mode the
-        // MC*NP old values are all requested before the first store.
-        constexpr int MC = NP == 1 ? 8 : 4;
+        // Detection and store: written (first buffer of an integration) or
+        // added in L2 (later buffers), one value per bin and plane.
 #pragma unroll
-        for (int m0 = 0; m0 < R; m0 += MC) {
-          float old[MC][NP];
-          if (a.mode == ACC_ADD) {
+        for (int m = 0; m < R; ++m) {
+          float acc[NP];
+          if constexpr (POL == POL_TP) {
+            acc[0] = tp[m];
+          } else {
 #pragma unroll
-            for (int mm = 0; mm < MC; ++mm) {
-              const int pos = out_pos(k2 + N2 * (j + (m0 + mm) * T), N, a.inverse);
-#pragma unroll
-              for (int p = 0; p < NP; ++p) old[mm][p] = ld_f_hint(obase + p * plane + pos, pol_first);
-            }
+            for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
+            const float2 x[2] = {x0[m], v[0][m]};
+            detect_acc<POL, 2>(acc, x, im_sign);
           }
+          const int pos = out_pos(k2 + N2 * (j + m * T), N, a.inverse);
 #pragma unroll
-          for (int mm = 0; mm < MC; ++mm) {
-            const int m = m0 + mm;
-            float acc[NP];
-            if constexpr (POL == POL_TP) {
-              acc[0] = tp[m];
-            } else {
-#pragma unroll
-              for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
-              const float2 x[2] = {x0[m], v[0][m]};
-              detect_acc<POL, 2>(acc, x, im_sign);
-            }
-            const int pos = out_pos(k2 + N2 * (j + m * T), N, a.inverse);
-#pragma unroll
-            for (int p = 0; p < NP; ++p) {
-              const float val = a.mode == ACC_ADD ? __fmaf_rn(acc[p], a.scale, old[mm][p]) : acc[p] * a.scale;
-              st_f_hint(obase + p * plane + pos, val, pol_first);
-            }
+          for (int p = 0; p < NP; ++p) {
+            if (a.mode == ACC_ADD)
+              red_add_f_hint(obase + p * plane + pos, acc[p] * a.scale, pol_first);
+            else
+              st_f_hint(obase + p * plane + pos, acc[p] * a.scale, pol_first);
           }
         }
       }
