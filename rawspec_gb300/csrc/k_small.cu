@@ -105,27 +105,59 @@ k_small(SmallLaunch a) {
 
   float2* my_xch = xch + (size_t)g * NV * smem_padded_len(N);
 
+  using W = typename SampleWord<FMT, NV>::type;
+  constexpr bool kVec = T == 1 && (R * sizeof(W)) % 16 == 0;
+  // Words of spectrum `it` of this group (zeros past the unit's end).
+  auto load_words = [&](int it, W (&w)[R]) {
+    const int s_local = s_begin + gi + it * gps;
+    if (!(unit_ok && s_local < s_end)) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) w[m] = W{};
+      return;
+    }
+    const W* src = reinterpret_cast<const W*>(a.in) + chan_base + (unit_first_spec + s_local) * N + j;
+    if (kVec && a.vec16) {
+      // one thread per transform: its R contiguous words in 16-byte loads
+      const uint4* s4 = reinterpret_cast<const uint4*>(src);
+#pragma unroll
+      for (int i = 0; i < (int)(R * sizeof(W) / 16); ++i) {
+        const uint4 u = __ldg(s4 + i);
+        memcpy(reinterpret_cast<char*>(w) + 16 * i, &u, 16);
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < R; ++m) w[m] = __ldg(src + m * T);
+    }
+  };
+  // The next spectrum's words are requested before the current transform
+  // when the registers allow it (spectra of one thread, or 8 values per
+  // thread); otherwise each spectrum is loaded when it is processed.
+  constexpr bool kPrefetch = T == 1 || (NV == 2 ? R <= 8 : R <= 16);
+  static_assert(kPrefetch || !kVec, "vector loads only on the prefetching path");
+  W wn[kPrefetch ? R : 1];
+  if constexpr (kPrefetch) load_words(0, wn);
+
   for (int it = 0; it < iters; ++it) {
     const int s_local = s_begin + gi + it * gps;
     const bool valid = unit_ok && s_local < s_end;
     float2 v[NV][R];
-    if (valid) {
-      using W = typename SampleWord<FMT, NV>::type;
+    if constexpr (kPrefetch) {
+      W w[R];
+#pragma unroll
+      for (int m = 0; m < R; ++m) w[m] = wn[m];
+      if (it + 1 < iters) load_words(it + 1, wn);
+#pragma unroll
+      for (int m = 0; m < R; ++m) {
+        float2 smp[NV];
+        Unpack<FMT, NV>::run(w[m], smp);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q][m] = smp[q];
+      }
+    } else if (valid) {
       const W* src = reinterpret_cast<const W*>(a.in) + chan_base + (unit_first_spec + s_local) * N + j;
       W w[R];
-      constexpr bool kVec = T == 1 && (R * sizeof(W)) % 16 == 0;
-      if (kVec && a.vec16) {
-        // one thread per transform: its R contiguous words in 16-byte loads
-        const uint4* s4 = reinterpret_cast<const uint4*>(src);
 #pragma unroll
-        for (int i = 0; i < (int)(R * sizeof(W) / 16); ++i) {
-          const uint4 u = __ldg(s4 + i);
-          memcpy(reinterpret_cast<char*>(w) + 16 * i, &u, 16);
-        }
-      } else {
-#pragma unroll
-        for (int m = 0; m < R; ++m) w[m] = __ldg(src + m * T);
-      }
+      for (int m = 0; m < R; ++m) w[m] = __ldg(src + m * T);
 #pragma unroll
       for (int m = 0; m < R; ++m) {
         float2 smp[NV];
