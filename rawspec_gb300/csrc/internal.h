@@ -104,6 +104,7 @@ struct LargeLaunch {
   int slab0 = 0;                  // first slab of this launch
   int unit0 = 0, unit_count = 0;  // units of this launch (two-kernel path)
   int ring = 0;                   // intermediate slots
+  int lag = 2;                    // row tiles of slab s follow the column tiles of slab s + lag
   int* ctl = nullptr;             // [0] error, [1] item counter, [2..2+S) A done, [2+S..2+2S) B done
   int fused_ctas = 0;             // persistent grid size
   // fused kernel: tensor maps of the input (rows of N1 words), of the
@@ -125,11 +126,12 @@ cudaError_t large_launch_b(const LargeLaunch& L, cudaStream_t s);
 cudaError_t large_prepare(const LargeLaunch& L);
 // Persistent fused variant (k_large_fused.cu): supported for 8-bit input of
 // two polarisations, 2^16 <= N <= 2^22 and integration units of one
-// spectrum; needs a ring of
-// large_fused_ring() intermediate slabs and large_fused_ctl_ints() control
-// words (zeroed once before the first launch).
+// spectrum.  large_fused_plan() sets the grid size, the lag and the number of
+// intermediate slabs (ring); the launch needs ring * 2 * N float2 of scratch
+// and large_fused_ctl_ints() control words (zeroed once before the first
+// launch).
 bool large_fused_supported(const LargeLaunch& L);
-int large_fused_ring();
+cudaError_t large_fused_plan(LargeLaunch& L);
 int large_fused_row_radix(int pol);  // radix of the row tiles (twiddle table of twN1)
 int large_fused_col_radix();         // radix of the column tiles (tables twN2 and twM)
 int large_fused_ctl_ints(const LargeLaunch& L);

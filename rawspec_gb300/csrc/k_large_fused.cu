@@ -10,7 +10,7 @@
 //
 // where A(s) are the column tiles of slab s (one channel-spectrum, both
 // polarisations) and B(s) its row tiles.  A(s) writes the FP32 intermediate
-// into slot s mod RING of a small ring (RING slabs, sized to stay in L2);
+// into slot s mod RING of a ring of RING slabs;
 // B(s) waits until every A(s) tile is published, A(s) waits until every
 // B(s-RING) tile has released the slot.  An item only ever waits for items
 // earlier in the order, which were taken by CTAs that are running, so the
@@ -43,19 +43,12 @@ namespace rsg {
 namespace {
 
 constexpr int kFusedTPB = 256;
-#ifndef RSG_FUSED_LAG
-#define RSG_FUSED_LAG 2
-#endif
-#ifndef RSG_FUSED_RING
-#define RSG_FUSED_RING 4
-#endif
-// Row tiles of slab s are queued after the column tiles of slab s + kLag, so
-// that a row tile rarely finds its slab's column tiles still running; a slot
-// of the intermediate ring is reused kRingSlots slabs later (> kLag keeps
-// every wait pointed at earlier items).
-constexpr int kLag = RSG_FUSED_LAG;
-constexpr int kRingSlots = RSG_FUSED_RING;
-static_assert(kRingSlots > kLag, "a slot must be released by row tiles queued before its next column tiles");
+// Row tiles of slab s are queued after the column tiles of slab s + lag, and
+// a slot of the intermediate ring is reused `ring` slabs later (ring > lag
+// keeps every wait pointed at earlier items).  Both distances are chosen at
+// plan time (large_fused_plan) to exceed the items in flight, so that a row
+// tile rarely finds its column tiles still running and a column tile rarely
+// finds its slot still in use.
 #ifndef RSG_FUSED_K
 #define RSG_FUSED_K 2
 #endif
@@ -273,10 +266,10 @@ struct Item {
   bool isA;
   int slab, titem;
 };
-__device__ __forceinline__ Item decode_item(long long item, int S, int itemsA, int itemsB) {
+__device__ __forceinline__ Item decode_item(long long item, int S, int lag, int itemsA, int itemsB) {
   Item it;
-  const int p1 = S < kLag ? S : kLag;       // A-only segments
-  const int mid = S > kLag ? S - kLag : 0;  // A+B segments
+  const int p1 = S < lag ? S : lag;       // A-only segments
+  const int mid = S > lag ? S - lag : 0;  // A+B segments
   const long long n1 = (long long)p1 * itemsA;
   const long long n2 = (long long)mid * (itemsA + itemsB);
   if (item < n1) {
@@ -285,10 +278,10 @@ __device__ __forceinline__ Item decode_item(long long item, int S, int itemsA, i
     it.titem = (int)(item % itemsA);
   } else if (item < n1 + n2) {
     const long long i2 = item - n1;
-    const int k = kLag + (int)(i2 / (itemsA + itemsB));
+    const int k = lag + (int)(i2 / (itemsA + itemsB));
     const int r = (int)(i2 % (itemsA + itemsB));
     it.isA = r < itemsA;
-    it.slab = it.isA ? k : k - kLag;
+    it.slab = it.isA ? k : k - lag;
     it.titem = it.isA ? r : r - itemsA;
   } else {  // B-only tail
     const long long i3 = item - n1 - n2;
@@ -387,7 +380,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
     const int pre = s_pre;
     __syncthreads();
     if (item >= total) break;
-    const Item it = decode_item(item, S, itemsA, itemsB);
+    const Item it = decode_item(item, S, a.lag, itemsA, itemsB);
     long long nxt = 0;
     if (tid == 0) {
       nxt = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
@@ -408,7 +401,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         return;
       }
       if (nxt >= total) return;
-      const Item nit = decode_item(nxt, S, itemsA, itemsB);
+      const Item nit = decode_item(nxt, S, a.lag, itemsA, itemsB);
       if (s + 2 == nstages) pre_ok = nit.isA || load_acquire(doneA + nit.slab) >= tilesA;
       if (pre_ok) {
         fence_proxy_async();
@@ -673,7 +666,32 @@ bool large_fused_supported(const LargeLaunch& L) {
   return L.chan_stride % n1 == 0 && (reinterpret_cast<uintptr_t>(L.in) & 15) == 0;
 }
 
-int large_fused_ring() { return kRingSlots; }
+cudaError_t large_fused_plan(LargeLaunch& L) {
+  cudaError_t e = fused_dispatch(L, nullptr, 1, nullptr);  // shared-memory limit first: occupancy depends on it
+  if (e != cudaSuccess) return e;
+  e = fused_dispatch(L, nullptr, 2, &L.fused_ctas);
+  if (e != cudaSuccess) return e;
+  int geo[8] = {0};
+  e = fused_dispatch(L, nullptr, 3, geo);
+  if (e != cudaSuccess) return e;
+  // Items in flight: two per CTA (the one it works on and the one it has
+  // taken ahead).  A segment of the order holds one slab's column and row
+  // items; lag and ring - lag both span at least the items in flight.
+  const int CA = geo[2], CB = geo[5];
+  const long long seg = (long long)((1 << L.logN1) / CA + (1 << L.logN2) / CB) / kTilesPerItem;
+  const int d = (int)((2ll * L.fused_ctas + seg - 1) / seg);
+#ifdef RSG_FUSED_LAG
+  L.lag = RSG_FUSED_LAG;
+#else
+  L.lag = std::max(2, d);
+#endif
+#ifdef RSG_FUSED_RING
+  L.ring = RSG_FUSED_RING;
+#else
+  L.ring = std::max(L.lag + 2, L.lag + d);
+#endif
+  return L.ring > L.lag ? cudaSuccess : cudaErrorInvalidValue;
+}
 
 int large_fused_row_radix(int pol) { return pol == POL_TP ? fused_rb<POL_TP>() : fused_rb<POL_FULL>(); }
 

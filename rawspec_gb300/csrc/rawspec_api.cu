@@ -699,8 +699,9 @@ int rawspec_initialize(rawspec_context* ctx) {
       if (large_fused_supported(L)) {
         P.fused = true;
         L.S = (int)ctx->Nc * (int)P.Nss;
-        L.ring = large_fused_ring();
-        sf = (size_t)L.ring * L.nv * ((size_t)1 << L.logN);
+        CK(large_fused_plan(L));
+        // slots in use: slab mod ring over at most S slabs
+        sf = (size_t)std::min(L.ring, L.S) * L.nv * ((size_t)1 << L.logN);
         pf = 0;
         const size_t nctl = (size_t)large_fused_ctl_ints(L);
         if (dev_alloc(g, &P.d_ctl, nctl * sizeof(int))) FAIL();

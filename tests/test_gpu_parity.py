@@ -97,8 +97,8 @@ def test_large_single_polarisation(cuda_device):
 @pytest.mark.parametrize("npol,conj,fft_dir", [(1, 0, 1), (4, 1, -1), (-4, 1, 1)])
 def test_fused_long_fft_many_slabs(cuda_device, npol, conj, fft_dir):
     # 2^16-point FFTs, one spectrum per integration, 4 spectra per channel
-    # and 3 channels: 12 slabs pass through the 4-slot intermediate ring of
-    # the persistent kernel, so slot reuse and both dependency waits occur.
+    # and 3 channels: 12 slabs, fewer than the lag the plan chooses for this
+    # length, so every column tile is queued before the first row tile.
     nt, Ntpb = 1 << 16, 1 << 18
     c = dict(Nc=3, Np=2, Ntpb=Ntpb, nbits=8, nblocks=1, products=[(nt, 1, npol)], conj=conj, fft_dir=fft_dir)
     blocks = synth.gaussian_blocks(1, 3, Ntpb, 2, sigma=20.0, seed=300 + npol)
@@ -106,6 +106,21 @@ def test_fused_long_fft_many_slabs(cuda_device, npol, conj, fft_dir):
     ref, _ = oracle_for(c, blocks)
     assert dumps[0].shape == ref[0].shape
     assert normalized_error(dumps[0], ref[0], npol, 3, nt) < REL_TOL
+
+
+@pytest.mark.parametrize("npol", [1, 4, -4])
+def test_fused_ring_slot_reuse(cuda_device, npol):
+    # 2^20-point FFTs, one spectrum per integration, 2 spectra per channel and
+    # 5 channels: the 10 slabs outnumber the intermediate ring the plan sizes
+    # for this length (6 slabs on a 152-SM GPU), so slots are reused and the
+    # column tiles of a slab wait for the row tiles of an earlier one.
+    nt, Ntpb = 1 << 20, 1 << 21
+    c = dict(Nc=5, Np=2, Ntpb=Ntpb, nbits=8, nblocks=1, products=[(nt, 1, npol)], conj=0, fft_dir=1)
+    blocks = synth.gaussian_blocks(1, 5, Ntpb, 2, sigma=20.0, seed=350 - npol)
+    dumps, _, _, _ = run_gpu(c, blocks)
+    ref, _ = oracle_for(c, blocks)
+    assert dumps[0].shape == ref[0].shape
+    assert normalized_error(dumps[0], ref[0], npol, 5, nt) < REL_TOL
 
 
 def test_inverse_direction_and_nis_chunks(cuda_device):
