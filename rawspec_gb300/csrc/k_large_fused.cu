@@ -49,11 +49,17 @@ constexpr int kFusedTPB = 256;
 // plan time (large_fused_plan) to exceed the items in flight, so that a row
 // tile rarely finds its column tiles still running and a column tile rarely
 // finds its slot still in use.
-#ifndef RSG_FUSED_K
-#define RSG_FUSED_K 2
+// Tiles per work item (amortises the item overheads): 4 in total-power mode,
+// 2 in the cross-pol modes (measured best on GB300 at 2^20).
+#ifndef RSG_FUSED_K_TP
+#define RSG_FUSED_K_TP 4
 #endif
-constexpr int kTilesPerItem = RSG_FUSED_K;  // tiles per work item (amortises the item overheads)
-static_assert(kTilesPerItem >= 2, "an item must fill both stage buffers");
+#ifndef RSG_FUSED_K_X
+#define RSG_FUSED_K_X 2
+#endif
+template <int POL>
+__host__ __device__ constexpr int fused_k() { return POL == POL_TP ? RSG_FUSED_K_TP : RSG_FUSED_K_X; }
+static_assert(fused_k<POL_TP>() >= 2 && fused_k<POL_FULL>() >= 2, "an item must fill both stage buffers");
 #ifndef RSG_FUSED_DISCARD
 #define RSG_FUSED_DISCARD 1
 #endif
@@ -304,7 +310,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
   static_assert(!TOUT || F::TMA_OUT, "tensor-store outputs need one plane and 16-byte rows");
   constexpr int N = N1 * N2;
   constexpr int NP = PolOut<POL>::NP;
-  constexpr int K = kTilesPerItem;
+  constexpr int K = fused_k<POL>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* twA = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   float2* twB = twA + F::OFF_TWB;
@@ -615,6 +621,7 @@ cudaError_t fused_t(const LargeLaunch& L, cudaStream_t s, int mode_op, int* ctas
     ctas_out[5] = F::CB;
     ctas_out[6] = F::BOXO;
     ctas_out[7] = F::TMA_OUT ? 1 : 0;
+    ctas_out[8] = fused_k<POL>();
     return cudaSuccess;
   }
   k<<<L.fused_ctas, kFusedTPB, F::SMEM, s>>>(L);
@@ -671,14 +678,14 @@ cudaError_t large_fused_plan(LargeLaunch& L) {
   if (e != cudaSuccess) return e;
   e = fused_dispatch(L, nullptr, 2, &L.fused_ctas);
   if (e != cudaSuccess) return e;
-  int geo[8] = {0};
+  int geo[9] = {0};
   e = fused_dispatch(L, nullptr, 3, geo);
   if (e != cudaSuccess) return e;
   // Items in flight: two per CTA (the one it works on and the one it has
   // taken ahead).  A segment of the order holds one slab's column and row
   // items; lag and ring - lag both span at least the items in flight.
   const int CA = geo[2], CB = geo[5];
-  const long long seg = (long long)((1 << L.logN1) / CA + (1 << L.logN2) / CB) / kTilesPerItem;
+  const long long seg = (long long)((1 << L.logN1) / CA + (1 << L.logN2) / CB) / geo[8];
   const int d = (int)((2ll * L.fused_ctas + seg - 1) / seg);
 #ifdef RSG_FUSED_LAG
   L.lag = RSG_FUSED_LAG;
@@ -728,7 +735,7 @@ cudaError_t large_fused_prepare(LargeLaunch& L) {
   if (e != cudaSuccess) return e;
   e = fused_dispatch(L, nullptr, 2, &L.fused_ctas);
   if (e != cudaSuccess) return e;
-  int geo[8] = {0};
+  int geo[9] = {0};
   e = fused_dispatch(L, nullptr, 3, geo);
   if (e != cudaSuccess) return e;
   const int CW = geo[0], BOXR = geo[1], CA = geo[2], TA = geo[3], RA = geo[4], CB = geo[5], BOXO = geo[6];
