@@ -387,17 +387,15 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
     __syncthreads();
     if (item >= total) break;
     const Item it = decode_item(item, S, a.lag, itemsA, itemsB);
-    long long nxt = 0;
-    if (tid == 0) {
-      nxt = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
-      s_next = nxt;
-      pre_ok = false;
-    }
+    long long nxt = total;
+    if (tid == 0) pre_ok = false;
     const int nstages = it.isA ? K : 2 * K;
     // Requests stage s + 2 into the buffer stage s has released: the item's
     // own, else the next item's first stages (B only once its column tiles
-    // are all published).  Called by every thread after a CTA barrier that
-    // follows the last use of the buffer.
+    // are all published).  The next item is taken here, when the first of
+    // them is due, so that each CTA holds little more than one item at a
+    // time.  Called by every thread after a CTA barrier that follows the last
+    // use of the buffer.
     auto refill = [&](int s) {
       if (tid != 0) return;
       const int buf = s & 1;
@@ -406,12 +404,17 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         issue_stage(it, s + 2, buf);
         return;
       }
-      if (nxt >= total) return;
-      const Item nit = decode_item(nxt, S, a.lag, itemsA, itemsB);
-      if (s + 2 == nstages) pre_ok = nit.isA || load_acquire(doneA + nit.slab) >= tilesA;
+      if (s + 2 == nstages) {
+        nxt = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
+        s_next = nxt;
+        if (nxt < total) {
+          const Item nit = decode_item(nxt, S, a.lag, itemsA, itemsB);
+          pre_ok = nit.isA || load_acquire(doneA + nit.slab) >= tilesA;
+        }
+      }
       if (pre_ok) {
         fence_proxy_async();
-        issue_stage(nit, s + 2 - nstages, buf);
+        issue_stage(decode_item(nxt, S, a.lag, itemsA, itemsB), s + 2 - nstages, buf);
       }
     };
 
@@ -681,12 +684,13 @@ cudaError_t large_fused_plan(LargeLaunch& L) {
   int geo[9] = {0};
   e = fused_dispatch(L, nullptr, 3, geo);
   if (e != cudaSuccess) return e;
-  // Items in flight: two per CTA (the one it works on and the one it has
-  // taken ahead).  A segment of the order holds one slab's column and row
-  // items; lag and ring - lag both span at least the items in flight.
+  // Items in flight: about 1.5 per CTA (the one it works on, and the next
+  // one, taken shortly before the current one ends).  A segment of the order
+  // holds one slab's column and row items; lag and ring - lag both span at
+  // least the items in flight.
   const int CA = geo[2], CB = geo[5];
   const long long seg = (long long)((1 << L.logN1) / CA + (1 << L.logN2) / CB) / geo[8];
-  const int d = (int)((2ll * L.fused_ctas + seg - 1) / seg);
+  const int d = (int)((3ll * L.fused_ctas / 2 + seg - 1) / seg);
 #ifdef RSG_FUSED_LAG
   L.lag = RSG_FUSED_LAG;
 #else
