@@ -94,7 +94,7 @@ def test_large_single_polarisation(cuda_device):
     assert normalized_error(dumps[0], ref[0], 1, 2, nt) < REL_TOL
 
 
-@pytest.mark.parametrize("npol,conj,fft_dir", [(1, 0, 1), (4, 1, -1), (-4, 1, 1)])
+@pytest.mark.parametrize("npol,conj,fft_dir", [(1, 0, 1), (1, 1, -1), (4, 1, -1), (-4, 1, 1)])
 def test_fused_long_fft_many_slabs(cuda_device, npol, conj, fft_dir):
     # 2^16-point FFTs, one spectrum per integration, 4 spectra per channel
     # and 3 channels: 12 slabs, fewer than the lag the plan chooses for this
@@ -121,6 +121,23 @@ def test_fused_ring_slot_reuse(cuda_device, npol):
     ref, _ = oracle_for(c, blocks)
     assert dumps[0].shape == ref[0].shape
     assert normalized_error(dumps[0], ref[0], npol, 5, nt) < REL_TOL
+
+
+def test_fused_with_incoherent_sum(cuda_device):
+    # two antennas of 3 channels, 2^16-point products on the fused path in
+    # total power and full Stokes, integrations spanning the 2 buffers, and
+    # the weighted sum over antennas of both
+    nt = 1 << 16
+    c = dict(Nc=6, Np=2, Ntpb=nt, nbits=8, nblocks=2, Nant=2, products=[(nt, 2, 1), (nt, 2, -4)], conj=0,
+             fft_dir=1)
+    blocks = synth.gaussian_blocks(2, 6, nt, 2, sigma=18.0, seed=410)
+    w = synth.weights(2, seed=411)
+    dumps, ics, _, _ = run_gpu(c, blocks, weights=w)
+    ref, ref_ics = oracle_for(c, blocks, weights=w)
+    for i, (_, _, npol) in enumerate(c["products"]):
+        assert dumps[i].shape == ref[i].shape
+        assert normalized_error(dumps[i], ref[i], npol, 6, nt) < REL_TOL
+        assert normalized_error(ics[i], ref_ics[i], npol, 3, nt) < REL_TOL
 
 
 def test_inverse_direction_and_nis_chunks(cuda_device):
