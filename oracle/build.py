@@ -5,6 +5,7 @@ rawspec_cpu.c (FP32 OpenMP chain used as the CPU baseline) with gcc.
 """
 from __future__ import annotations
 
+import fcntl
 import os
 import subprocess
 import sys
@@ -17,17 +18,31 @@ SRCS = [HERE / "rawspec_oracle.c", HERE / "rawspec_cpu.c"]
 DEPS = SRCS + [HERE / "rawspec_oracle.h", Path(__file__)]
 
 
+def _fresh() -> bool:
+    return LIB.exists() and all(p.stat().st_mtime <= LIB.stat().st_mtime for p in DEPS)
+
+
 def build(force: bool = False) -> Path:
-    if not force and LIB.exists() and all(p.stat().st_mtime <= LIB.stat().st_mtime for p in DEPS):
+    if not force and _fresh():
         return LIB
     BUILD.mkdir(exist_ok=True)
+    with open(BUILD / ".lock", "w") as fh:  # one builder at a time; the others find it fresh
+        fcntl.flock(fh, fcntl.LOCK_EX)
+        try:
+            if force or not _fresh():
+                _build()
+        finally:
+            fcntl.flock(fh, fcntl.LOCK_UN)
+    return LIB
+
+
+def _build() -> None:
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-shared", "-fopenmp", "-o", str(tmp), *map(str, SRCS), "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
-    return LIB
 
 
 if __name__ == "__main__":

@@ -8,6 +8,8 @@ statically, so the library depends on the driver only.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import contextlib
+import fcntl
 import os
 import shutil
 import subprocess
@@ -66,10 +68,30 @@ def _compile(src: Path, verbose: bool) -> Path:
     return obj
 
 
+@contextlib.contextmanager
+def _build_lock():
+    """Serialises builders (e.g. the ranks of a multi-process run that all
+    call build()): the second one waits, then finds the library up to date."""
+    BUILD.mkdir(exist_ok=True)
+    with open(BUILD / ".lock", "w") as fh:
+        fcntl.flock(fh, fcntl.LOCK_EX)
+        try:
+            yield
+        finally:
+            fcntl.flock(fh, fcntl.LOCK_UN)
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
     """Compiles librawspec.so if any source is newer than it; returns its path."""
     if not force and up_to_date():
         return LIB
+    with _build_lock():
+        if not force and up_to_date():
+            return LIB
+        return _build(verbose)
+
+
+def _build(verbose: bool) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
     srcs = _sources()
