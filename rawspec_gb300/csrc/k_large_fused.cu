@@ -441,11 +441,24 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         ph ^= 1u << buf;
         const int tile = it.titem * K + t;
         const int n1 = tile * C + col;
-        uint32_t w[R];
+        // polarisation 0 unpacked; polarisation 1 kept as packed bytes, two
+        // samples per register, while polarisation 0 is transformed
+        float2 v[1][R];
+        uint32_t p1[R / 2];
         {
           const uint32_t* words = reinterpret_cast<const uint32_t*>(sb) + ((tile * C) & 3) + col;
+          uint32_t prev = 0;
 #pragma unroll
-          for (int m = 0; m < R; ++m) w[m] = words[(j + T * m) * F::CW];
+          for (int m = 0; m < R; ++m) {
+            const uint32_t wm = words[(j + T * m) * F::CW];
+            float2 smp[2];
+            Unpack<FMT_I8, 2>::run(wm, smp);
+            v[0][m] = smp[0];
+            if (m & 1)
+              p1[m / 2] = __byte_perm(prev, wm, 0x7632);
+            else
+              prev = wm;
+          }
         }
         __syncthreads();  // the buffer becomes the exchange buffer; tile t-1 is done
         if (t > 0) refill(t - 1);
@@ -453,12 +466,13 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         float2* dst = scr + n1;
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-          float2 v[1][R];
+          if (q == 1) {
 #pragma unroll
-          for (int m = 0; m < R; ++m) {
-            float2 smp[2];
-            Unpack<FMT_I8, 2>::run(w[m], smp);
-            v[0][m] = smp[q];
+            for (int m = 0; m < R; ++m) {
+              float2 smp[1];
+              Unpack<FMT_I8, 1>::run((uint16_t)(m & 1 ? p1[m / 2] >> 16 : p1[m / 2] & 0xffffu), smp);
+              v[0][m] = smp[0];
+            }
           }
           GroupFFT<N2, R, 1>::run(v, j, sb + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
 #pragma unroll
