@@ -140,6 +140,25 @@ def test_fused_with_incoherent_sum(cuda_device):
         assert normalized_error(ics[i], ref_ics[i], npol, 3, nt) < REL_TOL
 
 
+@pytest.mark.parametrize("npol", [1, 4])
+def test_long_integration_3072_spectra(cuda_device, npol):
+    # Nint 3072 of 1024-point spectra spanning three 2-block buffers (the
+    # production's third product): the per-chunk register sums, the
+    # fixed-order chunk reduction and the accumulation across buffers stay
+    # within the FP32 tolerance of the FP64 oracle.
+    Nc, Ntpb = 2, 524288
+    c = dict(Nc=Nc, Np=2, Ntpb=Ntpb, nbits=8, nblocks=6, products=[(1024, 3072, npol), (1 << 20, 3, npol)],
+             conj=0, fft_dir=1)
+    blocks = synth.gaussian_blocks(6, Nc, Ntpb, 2, sigma=20.0, seed=500 + npol)
+    dumps, _, _, _ = run_gpu(c, blocks)
+    ref, _ = oracle_for(c, blocks)
+    for i, (nt, _, _) in enumerate(c["products"]):
+        assert dumps[i].shape == ref[i].shape == (1, abs(npol) * Nc * nt)
+        err = normalized_error(dumps[i], ref[i], npol, Nc, nt)
+        print(f"Nt {nt}, Npolout {npol}: normalized error {err:.2e}")
+        assert err < REL_TOL
+
+
 def test_inverse_direction_and_nis_chunks(cuda_device):
     c = dict(Nc=4, Np=2, Ntpb=8192, nbits=8, nblocks=6, products=[(1024, 24, -4), (8192, 3, 1)], conj=1, fft_dir=-1)
     blocks = synth.gaussian_blocks(6, 4, 8192, 2, sigma=20.0, seed=7)
