@@ -4,18 +4,19 @@
 //
 // The two passes of the four-step FFT (see k_large.cu) become work items of
 // one persistent kernel, taken in a fixed order through an atomic counter
-// (here with a lag of 2):
+// (shown for a lag of 2):
 //
 //   A(0) A(1) A(2) B(0) A(3) B(1) ... A(S-1) B(S-3) B(S-2) B(S-1)
 //
 // where A(s) are the column tiles of slab s (one channel-spectrum, both
 // polarisations) and B(s) its row tiles.  A(s) writes the FP32 intermediate
-// into slot s mod RING of a ring of RING slabs;
-// B(s) waits until every A(s) tile is published, A(s) waits until every
-// B(s-RING) tile has released the slot.  An item only ever waits for items
-// earlier in the order, which were taken by CTAs that are running, so the
-// waits always end; they are bounded nonetheless and record an error instead
-// of hanging if the bound is ever reached.
+// into slot s mod RING of a ring of RING slabs; B(s) waits until every A(s)
+// tile is published, A(s) waits until every B(s-RING) tile has released the
+// slot.  LAG and RING are chosen at plan time to cover the items in flight.
+// An item only ever waits for items earlier in the order, which were taken
+// by CTAs that are running, so the waits always end; they are bounded
+// nonetheless and record an error instead of hanging if the bound is ever
+// reached.
 //
 // Data movement.  Every tile's input reaches shared memory through the
 // copy engine of the SM (TMA), double-buffered: the column tiles' 8-bit
@@ -24,11 +25,11 @@
 // polarisation.  A stage's buffer becomes the transform's exchange buffer
 // once its values are in registers, and the next stage is requested as soon
 // as the transform is done with it; the first two stages of the CTA's next
-// work item are requested while the current one finishes (the item is taken
-// one ahead), so the loads of one item overlap the arithmetic of the other.
+// work item (taken at that moment) are requested while the current one
+// finishes, so the loads of one item overlap the arithmetic of the other.
 // Completion is tracked by two mbarriers (expected-transaction counts).
 // Intermediate rows are discarded from L2 once copied (they are dead), so
-// the ring is never written back to HBM.
+// rows still in L2 are never written back to HBM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
