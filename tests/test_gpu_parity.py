@@ -339,13 +339,13 @@ def test_unpack_matches_texture_unit(cuda_device, tmp_path):
     assert all(float(o8[i]) == O.snorm(int(np.int8(np.uint8(i))), 8) for i in range(256))
 
 
-@pytest.mark.parametrize("nbits", [8, 4])
-def test_combined_call_pipelines_copy_and_processing(cuda_device, nbits):
+@pytest.mark.parametrize("nbits,Nc", [(8, 8), (4, 8), (8, 13)])
+def test_combined_call_pipelines_copy_and_processing(cuda_device, nbits, Nc):
     # rawspec_copy_blocks_to_gpu_and_start_processing on buffers of 16 MiB
     # and more copies channel groups on a second stream and processes each
     # group as it lands; results must equal the separate calls' and the
-    # oracle's.
-    Nc, Ntpb, nblocks = 8, 1 << 19, 3
+    # oracle's.  13 channels make groups of one and two channels.
+    Ntpb, nblocks = 1 << 19, 3
     prods = [(1024, 16, 1), (1 << 16, 1, 4), (8, 128, -4)]
     if nbits == 4:
         blocks, _ = synth.int4_blocks(nblocks, Nc, Ntpb, 2, Nant=1, seed=41)
