@@ -15,6 +15,7 @@
 // Nothing but the raw voltages is read and nothing but integrated spectra is
 // written.
 #include <algorithm>
+#include <cmath>
 
 #include "detect.cuh"
 #include "fft_core.cuh"
@@ -275,11 +276,15 @@ SmallInfo small_info_dyn(int logN, int nv, int pol) {
   }
 }
 
+// op: 0 launch, 1 allow the dynamic shared memory, 2 also report the
+// resident CTAs per SM in *occ.
 template <int N, int FMT, int NV, int POL>
-cudaError_t launch_t(const SmallLaunch& L, cudaStream_t s, bool prep) {
+cudaError_t launch_t(const SmallLaunch& L, cudaStream_t s, int op, int* occ) {
   auto k = k_small<N, FMT, NV, POL>;
-  if (prep) {  // preparation call: allow the dynamic shared memory
-    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+  if (op != 0) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+    if (e != cudaSuccess || op == 1) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k, SmallCfg<N, PolOut<POL>::NP>::TPB, L.smem);
   }
   const int grid = ((L.unit_count + L.sets - 1) / L.sets) * L.chunks;
   if (grid < 1) return cudaSuccess;
@@ -288,18 +293,58 @@ cudaError_t launch_t(const SmallLaunch& L, cudaStream_t s, bool prep) {
 }
 
 template <int N, int FMT>
-cudaError_t launch_pol(const SmallLaunch& L, cudaStream_t s, bool prep) {
-  if (L.nv == 1) return launch_t<N, FMT, 1, POL_TP>(L, s, prep);
+cudaError_t launch_pol(const SmallLaunch& L, cudaStream_t s, int op, int* occ) {
+  if (L.nv == 1) return launch_t<N, FMT, 1, POL_TP>(L, s, op, occ);
   switch (L.pol) {
-    case POL_FULL: return launch_t<N, FMT, 2, POL_FULL>(L, s, prep);
-    case POL_STOKES: return launch_t<N, FMT, 2, POL_STOKES>(L, s, prep);
-    default: return launch_t<N, FMT, 2, POL_TP>(L, s, prep);
+    case POL_FULL: return launch_t<N, FMT, 2, POL_FULL>(L, s, op, occ);
+    case POL_STOKES: return launch_t<N, FMT, 2, POL_STOKES>(L, s, op, occ);
+    default: return launch_t<N, FMT, 2, POL_TP>(L, s, op, occ);
   }
 }
 
 template <int N>
-cudaError_t launch_fmt(const SmallLaunch& L, cudaStream_t s, bool prep) {
-  return L.fmt == FMT_I16 ? launch_pol<N, FMT_I16>(L, s, prep) : launch_pol<N, FMT_I8>(L, s, prep);
+cudaError_t launch_fmt(const SmallLaunch& L, cudaStream_t s, int op, int* occ) {
+  return L.fmt == FMT_I16 ? launch_pol<N, FMT_I16>(L, s, op, occ) : launch_pol<N, FMT_I8>(L, s, op, occ);
+}
+
+cudaError_t small_dispatch(const SmallLaunch& L, cudaStream_t s, int op, int* occ = nullptr) {
+  switch (L.logN) {
+    case 0: return launch_fmt<1>(L, s, op, occ);
+    case 1: return launch_fmt<2>(L, s, op, occ);
+    case 2: return launch_fmt<4>(L, s, op, occ);
+    case 3: return launch_fmt<8>(L, s, op, occ);
+    case 4: return launch_fmt<16>(L, s, op, occ);
+    case 5: return launch_fmt<32>(L, s, op, occ);
+    case 6: return launch_fmt<64>(L, s, op, occ);
+    case 7: return launch_fmt<128>(L, s, op, occ);
+    case 8: return launch_fmt<256>(L, s, op, occ);
+    case 9: return launch_fmt<512>(L, s, op, occ);
+    case 10: return launch_fmt<1024>(L, s, op, occ);
+    case 11: return launch_fmt<2048>(L, s, op, occ);
+    case 12: return launch_fmt<4096>(L, s, op, occ);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Chunks per unit: at least c_min (the parallelism asked for), raised while
+// that makes the grid fill its last wave of resident CTAs markedly better
+// (all CTAs of a launch take about the same time, so a grid of 2.1 waves
+// runs as long as one of 3).  Units processed whole (c_min = 1) stay whole:
+// splitting them would add a finalisation pass.
+#ifndef RSG_SMALL_WAVEFIT
+#define RSG_SMALL_WAVEFIT 1
+#endif
+int fit_chunks(int M, int ublocks, int c_min, int max_chunks, int slots) {
+  auto actual = [&](int c) { const int spc = (M + c - 1) / c; return (M + spc - 1) / spc; };
+  auto eff = [&](int c) {
+    const double w = (double)ublocks * actual(c) / slots;
+    return w / std::ceil(w);
+  };
+  int best = std::max(1, std::min(c_min, max_chunks));
+  if (!RSG_SMALL_WAVEFIT || slots <= 0 || best == 1) return best;
+  for (int c = best + 1; c <= std::min(max_chunks, 2 * best); ++c)
+    if (eff(c) > eff(best) + 0.05) best = c;
+  return best;
 }
 
 }  // namespace
@@ -320,8 +365,13 @@ int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats, int
   L.sets = G / gps;
   const int ublocks = (L.n_units + L.sets - 1) / L.sets;
   const int max_chunks = (L.M + gps - 1) / gps;
-  int chunks = (target_ctas + ublocks - 1) / ublocks;
-  chunks = std::max(1, std::min(chunks, max_chunks));
+  // resident CTAs on the device
+  int occ = 0, sms = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+      cudaSuccess || small_dispatch(L, nullptr, 2, &occ) != cudaSuccess)
+    occ = 0;
+  const int slots = occ * sms;
+  const int chunks = fit_chunks(L.M, ublocks, (target_ctas + ublocks - 1) / ublocks, max_chunks, slots);
   L.spc = (L.M + chunks - 1) / chunks;
   L.chunks = (L.M + L.spc - 1) / L.spc;
   L.grid = ublocks * L.chunks;
@@ -329,8 +379,7 @@ int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats, int
   {
     const int gunits = std::max(1, L.n_units / std::max(1, pipe_groups));
     const int gublocks = (gunits + L.sets - 1) / L.sets;
-    int c2 = (target_ctas + gublocks - 1) / gublocks;
-    c2 = std::max(1, std::min(c2, max_chunks));
+    const int c2 = fit_chunks(L.M, gublocks, (target_ctas + gublocks - 1) / gublocks, max_chunks, slots);
     L.spc_pipe = (L.M + c2 - 1) / c2;
     L.chunks_pipe = (L.M + L.spc_pipe - 1) / L.spc_pipe;
   }
@@ -343,27 +392,8 @@ int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats, int
   return 0;
 }
 
-static cudaError_t small_dispatch(const SmallLaunch& L, cudaStream_t s, bool prep) {
-  switch (L.logN) {
-    case 0: return launch_fmt<1>(L, s, prep);
-    case 1: return launch_fmt<2>(L, s, prep);
-    case 2: return launch_fmt<4>(L, s, prep);
-    case 3: return launch_fmt<8>(L, s, prep);
-    case 4: return launch_fmt<16>(L, s, prep);
-    case 5: return launch_fmt<32>(L, s, prep);
-    case 6: return launch_fmt<64>(L, s, prep);
-    case 7: return launch_fmt<128>(L, s, prep);
-    case 8: return launch_fmt<256>(L, s, prep);
-    case 9: return launch_fmt<512>(L, s, prep);
-    case 10: return launch_fmt<1024>(L, s, prep);
-    case 11: return launch_fmt<2048>(L, s, prep);
-    case 12: return launch_fmt<4096>(L, s, prep);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-cudaError_t small_prepare(const SmallLaunch& L) { return small_dispatch(L, nullptr, true); }
-cudaError_t small_launch(const SmallLaunch& L, cudaStream_t s) { return small_dispatch(L, s, false); }
+cudaError_t small_prepare(const SmallLaunch& L) { return small_dispatch(L, nullptr, 1); }
+cudaError_t small_launch(const SmallLaunch& L, cudaStream_t s) { return small_dispatch(L, s, 0); }
 
 cudaError_t finalize_launch(const FinalizeLaunch& L, cudaStream_t s) {
   const long long total = (long long)L.n_units * L.np * L.N;
