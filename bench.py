@@ -14,7 +14,9 @@ Metric: RAW-in GB/s (RAW bytes of the step / step time).
   e2e    through the C-ABI from pinned host blocks, the reference CLI's
          per-buffer sequence: K x (rawspec_wait_for_completion +
          rawspec_copy_blocks_to_gpu_and_start_processing), then a final
-         wait; wall clock.
+         wait; wall clock; buffer_ms_p50 / buffer_ms_p99 are the
+         percentiles of one loop iteration (the wait for the previous buffer
+         and the copy and start of this one).
 
 `--impl reference` times the CPU restatement of the same chain (the
 reference has no CPU implementation of its spectrometer; the OpenMP FP32
@@ -301,15 +303,17 @@ def run_native(args, rank, world, local_rank):
             nbuf += 1
         sizes = [spec.ctx.h_pwrbuf_size[i] for i in range(3)]
         nis = [spec.product_info(i)[1] for i in range(3)]
-        reps, d2h = [], 0
+        reps, d2h, step_ms = [], 0, []
         for _ in range(E2E_REPS):
             barrier()
             t0 = time.perf_counter()
             for _ in range(args.steps):
+                ts = time.perf_counter()
                 if lib.rawspec_wait_for_completion(cp) != 0:
                     raise RuntimeError("wait failed")
                 if lib.rawspec_copy_blocks_to_gpu_and_start_processing(cp, 2, 0, 1) != 0:
                     raise RuntimeError("copy/start failed")
+                step_ms.append(1e3 * (time.perf_counter() - ts))
             if lib.rawspec_wait_for_completion(cp) != 0:
                 raise RuntimeError("wait failed")
             reps.append(max_over_ranks(time.perf_counter() - t0))
@@ -327,6 +331,7 @@ def run_native(args, rank, world, local_rank):
         clocks["window"] = "device-resident and end-to-end timed legs, with the profiling pass between them"
         results[npol] = dict(ms=ms, ms_serial=ms_serial, prof=prof, launches=launches, clocks=clocks, e2e_s=e2e_s,
                              e2e_samples=[whole_job_gbs(world, 2 * BLOCK_BYTES, args.steps, x) for x in reps],
+                             step_p50=float(np.percentile(step_ms, 50)), step_p99=float(np.percentile(step_ms, 99)),
                              d2h=d2h / args.steps, device_bytes=int(lib.rawspec_gb300_device_bytes(cp)))
         spec.close()
 
@@ -382,6 +387,7 @@ def run_native(args, rank, world, local_rank):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": step_bytes,
                 "d2h_bytes_per_step": int(r["d2h"]), "samples": r["e2e_samples"],
+                "buffer_ms_p50": r["step_p50"], "buffer_ms_p99": r["step_p99"],
                 "timing": f"wall clock of K steps, median of {E2E_REPS} runs"},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
