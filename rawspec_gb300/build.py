@@ -37,12 +37,13 @@ def nvcc() -> str:
 
 
 def _sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    """CUDA translation units (nvcc) and host-only C files (the C compiler)."""
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.c"))
 
 
 def _deps() -> list[Path]:
-    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) +
-                  list(INCLUDE.glob("*.h")) + [Path(__file__)])
+    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.c")) + list(CSRC.glob("*.cuh")) +
+                  list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h")) + [Path(__file__)])
 
 
 def up_to_date() -> bool:
@@ -58,8 +59,12 @@ def _extra_flags() -> list[str]:
 
 
 def _compile(src: Path, verbose: bool) -> Path:
-    obj = BUILD / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *_extra_flags(), "-c", str(src), "-o", str(obj)]
+    obj = BUILD / (src.stem + src.suffix.replace(".", "_") + ".o")
+    if src.suffix == ".c":
+        cmd = [os.environ.get("CC", "gcc"), "-std=gnu11", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall",
+               f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)]
+    else:
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *_extra_flags(), "-c", str(src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), flush=True)
     res = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,93 @@
+"""GUPPI RAW in, SIGPROC filterbank out, through the GPU path: the ingest
+(include/rawspec_gb300_io.h) reads a two-file stem with a missing packet
+index and DIRECTIO padding, selects a channel range, puts in a zero block
+for the gap and hands full buffers to the library; the filterbank writer,
+installed as the dump callback, writes the dumps.  The files must hold
+exactly the dumps the library produces when fed the same block sequence
+directly."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from rawspec_gb300 import api, io
+
+pytestmark = pytest.mark.gpu
+
+OBSNCHAN, NP, NBITS, NTPB = 8, 2, 8, 8192
+SCHAN, NCHAN = 2, 4
+PRODUCTS = [(16384, 1, 1), (1024, 8, 4)]
+PKTIDX = [0, 64, 128, 256, 320]   # 192 is missing
+FILES = [(0, 3, False), (3, 5, True)]  # blocks of each file, DIRECTIO
+
+
+def _blocks():
+    rng = np.random.default_rng(17)
+    v = np.clip(np.rint(rng.standard_normal((len(PKTIDX), OBSNCHAN, NTPB, NP, 2)) * 20), -128, 127)
+    return v.astype(np.int8)
+
+
+def test_raw_stem_to_filterbank_files(cuda_device, tmp_path):
+    blocks = _blocks()
+    paths = []
+    for k, (a, b, dio) in enumerate(FILES):
+        p = tmp_path / f"stem.{k:04d}.raw"
+        io.write_raw_file(p, [blocks[i].view(np.uint8).reshape(-1) for i in range(a, b)], PKTIDX[a:b], OBSNCHAN, NP,
+                          NBITS, NTPB, directio=dio)
+        paths.append(p)
+
+    L = io.lib()
+    first = io.RawHeader()
+    fd = os.open(paths[0], os.O_RDONLY)
+    assert L.rawspec_gb300_raw_read_header(fd, C.byref(first)) > 0
+    os.close(fd)
+
+    ctx = api.RawspecContext()
+    expand4 = C.c_int(0)
+    assert L.rawspec_gb300_ingest_geometry(C.byref(first), SCHAN, NCHAN, C.byref(ctx), C.byref(expand4)) == 0
+    assert (ctx.Nc, ctx.Np, ctx.Ntpb, ctx.Nbps, ctx.input_conjugated, expand4.value) == (NCHAN, NP, NTPB, 8, 1, 0)
+    ctx.No = len(PRODUCTS)
+    for i, (nt, na, npol) in enumerate(PRODUCTS):
+        ctx.Nts[i], ctx.Nas[i], ctx.Npolout[i] = nt, na, npol
+    assert L.rawspec_initialize(C.byref(ctx)) == 0
+    writers = []
+    try:
+        for i in range(ctx.No):
+            h = io.FilHeader()
+            assert L.rawspec_gb300_fil_header_for_product(C.byref(first), C.byref(ctx), i, SCHAN, b"stem.0000.raw",
+                                                          C.byref(h)) == 0
+            w = L.rawspec_gb300_fil_writer_open(C.byref(ctx), i, C.byref(h), str(tmp_path).encode(), b"out", i, 0,
+                                                None)
+            assert w
+            writers.append((w, io.fil_header_bytes(h)))
+        arr = (C.c_void_p * len(writers))(*[w for w, _ in writers])
+        ctx.user_data = C.cast(arr, C.c_void_p)
+        ctx.dump_callback = C.cast(L.rawspec_gb300_fil_dump_callback, api.DUMP_CALLBACK)
+        plist = (C.c_char_p * len(paths))(*[str(p).encode() for p in paths])
+        st = io.IngestStats()
+        assert L.rawspec_gb300_ingest_files(C.byref(ctx), plist, len(paths), SCHAN, expand4.value, C.byref(st)) == 0
+        assert (st.blocks_read, st.blocks_zero, st.buffers, st.stop) == (5, 1, 3, 0)
+    finally:
+        for w, _ in writers:
+            assert L.rawspec_gb300_fil_writer_close(w) == 0
+        L.rawspec_cleanup(C.byref(ctx))
+
+    # the same block sequence, fed directly: data blocks and one zero block
+    seq = [blocks[0], blocks[1], blocks[2], np.zeros_like(blocks[0]), blocks[3], blocks[4]]
+    host = np.stack([b[SCHAN:SCHAN + NCHAN] for b in seq]).view(np.uint8).reshape(len(seq), -1)
+    spec = api.Spectrometer(NCHAN, NP, NTPB, 8, PRODUCTS, conj=1)
+    try:
+        spec.process(host, combined=True)
+        want = [np.concatenate([np.asarray(d, dtype=np.float32).reshape(-1) for d in spec.dumps[i]])
+                for i in range(len(PRODUCTS))]
+    finally:
+        spec.close()
+    for i, (_, hdr) in enumerate(writers):
+        raw = (tmp_path / f"out.rawspec.{i:04d}.fil").read_bytes()
+        assert raw[:len(hdr)] == hdr
+        got = np.frombuffer(raw[len(hdr):], dtype=np.float32)
+        assert got.size == want[i].size
+        np.testing.assert_array_equal(got, want[i])
