@@ -202,6 +202,71 @@ def cpu_baseline_leg(min_seconds: float = 12.0) -> dict:
                       f"total power, {secs:.1f} s"}
 
 
+def ingest_leg(nbuf: int = 4) -> dict:
+    """GUPPI RAW files -> librawspec -> SIGPROC filterbank files at the
+    production shape: a two-file stem of 2 * nbuf blocks (128 MiB each) in
+    /dev/shm (RAM-backed), streamed by rawspec_gb300_ingest_files with the
+    filterbank writer as the dump callback; RAW file bytes over wall clock."""
+    import ctypes as Cc
+    import tempfile
+
+    from rawspec_gb300 import api, io, synth
+    base = Path("/dev/shm") if Path("/dev/shm").is_dir() else Path(tempfile.gettempdir())
+    blocks = synth.gaussian_blocks(2, NC, NTPB, NP, sigma=SIGMA, seed=5)
+    L = io.lib()
+    with tempfile.TemporaryDirectory(dir=base) as d:
+        paths = []
+        per_file = nbuf  # blocks per file: 2 files of nbuf blocks = nbuf buffers
+        for k in range(2):
+            p = Path(d) / f"bench.{k:04d}.raw"
+            io.write_raw_file(p, [blocks[i % 2] for i in range(per_file)],
+                              [(k * per_file + i) * 32 for i in range(per_file)], NC, NP, NBITS, NTPB)
+            paths.append(p)
+        hdr = io.RawHeader()
+        fd = os.open(paths[0], os.O_RDONLY)
+        L.rawspec_gb300_raw_read_header(fd, Cc.byref(hdr))
+        os.close(fd)
+        ctx = api.RawspecContext()
+        e4 = Cc.c_int(0)
+        if L.rawspec_gb300_ingest_geometry(Cc.byref(hdr), 0, 0, Cc.byref(ctx), Cc.byref(e4)) != 0:
+            raise RuntimeError("ingest geometry")
+        ctx.No = len(PRODUCTS)
+        for i, (nt, na) in enumerate(PRODUCTS):
+            ctx.Nts[i], ctx.Nas[i], ctx.Npolout[i] = nt, na, 1
+        if L.rawspec_initialize(Cc.byref(ctx)) != 0:
+            raise RuntimeError("rawspec_initialize failed")
+        writers = []
+        try:
+            for i in range(ctx.No):
+                fh = io.FilHeader()
+                L.rawspec_gb300_fil_header_for_product(Cc.byref(hdr), Cc.byref(ctx), i, 0, b"bench.0000.raw",
+                                                       Cc.byref(fh))
+                w = L.rawspec_gb300_fil_writer_open(Cc.byref(ctx), i, Cc.byref(fh), d.encode(), b"bench", i, 0, None)
+                if not w:
+                    raise RuntimeError("filterbank writer")
+                writers.append(w)
+            arr = (Cc.c_void_p * len(writers))(*writers)
+            ctx.user_data = Cc.cast(arr, Cc.c_void_p)
+            ctx.dump_callback = Cc.cast(L.rawspec_gb300_fil_dump_callback, api.DUMP_CALLBACK)
+            plist = (Cc.c_char_p * 2)(*[str(p).encode() for p in paths])
+            st = io.IngestStats()
+            L.rawspec_gb300_ingest_files(Cc.byref(ctx), plist, 2, 0, 0, Cc.byref(st))  # warm-up (page cache, GPU)
+            t0 = time.perf_counter()
+            rc = L.rawspec_gb300_ingest_files(Cc.byref(ctx), plist, 2, 0, 0, Cc.byref(st))
+            dt = time.perf_counter() - t0
+            if rc != 0 or st.stop != 0:
+                raise RuntimeError("ingest failed")
+        finally:
+            for w in writers:
+                L.rawspec_gb300_fil_writer_close(w)
+            L.rawspec_cleanup(Cc.byref(ctx))
+        file_bytes = sum(p.stat().st_size for p in paths)
+    return {"value": file_bytes / dt / 1e9, "unit": "GB/s", "files": 2, "file_bytes": file_bytes,
+            "blocks": int(st.blocks_read), "buffers": int(st.buffers), "storage": str(base),
+            "timing": "wall clock of rawspec_gb300_ingest_files over the stem (warm page cache), filterbank "
+                      "files written by the dump callback"}
+
+
 def run_reference(args, rank, world):
     """CPU restatement of the chain (kind "port") with all host threads."""
     if rank != 0:
@@ -407,6 +472,8 @@ def run_native(args, rank, world, local_rank):
     }
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_leg()
+    if rank == 0 and world == 1 and not args.no_ingest:
+        line["ingest"] = ingest_leg()
     if rank == 0:
         print(json.dumps(line), flush=True)
     group.close()
@@ -420,6 +487,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-ingest", action="store_true", help="skip the RAW-file ingest leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local_rank = rank_info()

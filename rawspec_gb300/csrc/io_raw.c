@@ -14,6 +14,7 @@
 #include <errno.h>
 #include <fcntl.h>
 #include <limits.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -290,19 +291,139 @@ RSG_EXPORT int rawspec_gb300_ingest_geometry(const rawspec_gb300_raw_hdr *h, uns
   return 0;
 }
 
-/* Reads exactly n bytes (short only at end of file); returns bytes read or -1. */
-static ssize_t read_fully(int fd, void *buf, size_t n) {
+/* ---------------------------------------------------------------------------
+ * Block reads: a block's channel range is one contiguous byte range of the
+ * file, read (or zero-filled) by a small pool of threads in 4 KiB-aligned
+ * stripes with pread, so that the page-cache copies are not limited to one
+ * core.  RAWSPEC_GB300_INGEST_THREADS sets the pool size (default: the
+ * online CPUs, at most 16).
+ * ------------------------------------------------------------------------- */
+#define RSG_MAX_READERS 16
+
+typedef struct {
+  int nthreads;  /* readers taking part, the calling thread included */
+  int quit;
+  pthread_barrier_t start, done;
+  pthread_mutex_t gate_mu;
+  pthread_cond_t gate_cv;
+  int gate;      /* set once the barriers are sized for the readers that started */
+  pthread_t tid[RSG_MAX_READERS];
+  /* the current job */
+  int fd;
+  off_t off;
+  char *dst;
+  size_t bytes;
+  int zero;
+  size_t want[RSG_MAX_READERS], got[RSG_MAX_READERS];
+} ReaderPool;
+
+typedef struct {
+  ReaderPool *pool;
+  int k;
+} ReaderArg;
+
+static void do_stripe(ReaderPool *p, int k) {
+  const size_t a = (p->bytes * (size_t)k / (size_t)p->nthreads) & ~(size_t)4095;
+  const size_t b = k + 1 == p->nthreads ? p->bytes : (p->bytes * (size_t)(k + 1) / (size_t)p->nthreads) & ~(size_t)4095;
+  const size_t n = b > a ? b - a : 0;
   size_t got = 0;
-  while (got < n) {
-    const ssize_t r = read(fd, (char *)buf + got, n - got);
-    if (r < 0) {
-      if (errno == EINTR) continue;
-      return -1;
+  if (p->zero) {
+    memset(p->dst + a, 0, n);
+    got = n;
+  } else {
+    while (got < n) {
+      const ssize_t r = pread(p->fd, p->dst + a + got, n - got, p->off + (off_t)(a + got));
+      if (r < 0) {
+        if (errno == EINTR) continue;
+        break;
+      }
+      if (r == 0) break;
+      got += (size_t)r;
     }
-    if (r == 0) break;
-    got += (size_t)r;
   }
-  return (ssize_t)got;
+  p->want[k] = n;
+  p->got[k] = got;
+}
+
+static void *reader_main(void *arg) {
+  ReaderArg *ra = (ReaderArg *)arg;
+  ReaderPool *p = ra->pool;
+  pthread_mutex_lock(&p->gate_mu);
+  while (!p->gate) pthread_cond_wait(&p->gate_cv, &p->gate_mu);
+  pthread_mutex_unlock(&p->gate_mu);
+  for (;;) {
+    pthread_barrier_wait(&p->start);
+    if (p->quit) break;
+    do_stripe(p, ra->k);
+    pthread_barrier_wait(&p->done);
+  }
+  return NULL;
+}
+
+static void pool_start(ReaderPool *p, ReaderArg *args) {
+  memset(p, 0, sizeof(*p));
+  long n = sysconf(_SC_NPROCESSORS_ONLN);
+  const char *env = getenv("RAWSPEC_GB300_INGEST_THREADS");
+  if (env && atoi(env) > 0) n = atoi(env);
+  if (n < 1) n = 1;
+  if (n > RSG_MAX_READERS) n = RSG_MAX_READERS;
+  pthread_mutex_init(&p->gate_mu, NULL);
+  pthread_cond_init(&p->gate_cv, NULL);
+  /* start the readers; they wait at the gate until the barriers exist */
+  int started = 1;
+  for (int k = 1; k < n; ++k) {
+    args[k].pool = p;
+    args[k].k = k;
+    if (pthread_create(&p->tid[k], NULL, reader_main, &args[k]) != 0) break;
+    ++started;
+  }
+  p->nthreads = started;
+  if (started > 1) {
+    pthread_barrier_init(&p->start, NULL, (unsigned)started);
+    pthread_barrier_init(&p->done, NULL, (unsigned)started);
+  }
+  pthread_mutex_lock(&p->gate_mu);
+  p->gate = 1;
+  pthread_cond_broadcast(&p->gate_cv);
+  pthread_mutex_unlock(&p->gate_mu);
+}
+
+static void pool_stop(ReaderPool *p) {
+  if (p->nthreads > 1) {
+    p->quit = 1;
+    pthread_barrier_wait(&p->start);
+    for (int k = 1; k < p->nthreads; ++k) pthread_join(p->tid[k], NULL);
+    pthread_barrier_destroy(&p->start);
+    pthread_barrier_destroy(&p->done);
+  }
+  pthread_cond_destroy(&p->gate_cv);
+  pthread_mutex_destroy(&p->gate_mu);
+}
+
+/* Reads `bytes` at file offset `off` into dst (or zero-fills dst when fd < 0);
+ * returns 0 if every byte was read. */
+static int pool_read(ReaderPool *p, int fd, off_t off, char *dst, size_t bytes) {
+  p->fd = fd;
+  p->off = off;
+  p->dst = dst;
+  p->bytes = bytes;
+  p->zero = fd < 0;
+  if (p->nthreads > 1) pthread_barrier_wait(&p->start);
+  do_stripe(p, 0);
+  if (p->nthreads > 1) pthread_barrier_wait(&p->done);
+  for (int k = 0; k < p->nthreads; ++k)
+    if (p->got[k] != p->want[k]) return 1;
+  return 0;
+}
+
+/* Hands the host blocks to the GPU once block bi completes a buffer. */
+static int buffer_done(rawspec_context *ctx, long long bi, int expand4, rawspec_gb300_ingest_stats *st) {
+  if (bi % ctx->Nb != ctx->Nb - 1) return 0;
+  if (rawspec_wait_for_completion(ctx) != 0) return 1;
+  if (rawspec_copy_blocks_to_gpu_and_start_processing(ctx, ctx->Nb, (char)(expand4 ? 1 : 0), RAWSPEC_FORWARD_FFT) != 0)
+    return 1;
+  st->buffers++;
+  return 0;
 }
 
 RSG_EXPORT int rawspec_gb300_ingest_files(rawspec_context *ctx, const char *const *paths, int npaths, unsigned int schan,
@@ -318,21 +439,12 @@ RSG_EXPORT int rawspec_gb300_ingest_files(rawspec_context *ctx, const char *cons
   rawspec_gb300_pktidx_state ps;
   memset(&ps, 0, sizeof(ps));
   long long bi = 0;  /* block index across the stem */
-  int rc = 0;
+  int lib_error = 0;
+  ReaderPool pool;
+  ReaderArg args[RSG_MAX_READERS];
+  pool_start(&pool, args);
 
-  /* hands the host blocks to the GPU when block bi completes a buffer */
-#define RSG_BUFFER_DONE()                                                                            \
-  do {                                                                                               \
-    if (bi % ctx->Nb == ctx->Nb - 1) {                                                               \
-      if (rawspec_wait_for_completion(ctx) != 0) return 1;                                           \
-      if (rawspec_copy_blocks_to_gpu_and_start_processing(ctx, ctx->Nb, (char)(expand4 ? 1 : 0),    \
-                                                          RAWSPEC_FORWARD_FFT) != 0)                 \
-        return 1;                                                                                    \
-      st->buffers++;                                                                                 \
-    }                                                                                                \
-  } while (0)
-
-  for (int f = 0; f < npaths && st->stop == 0; ++f) {
+  for (int f = 0; f < npaths && st->stop == 0 && !lib_error; ++f) {
     const int fd = open(paths[f], O_RDONLY);
     if (fd < 0) {
       fprintf(stderr, "cannot open %s: %s\n", paths[f], strerror(errno));
@@ -341,7 +453,7 @@ RSG_EXPORT int rawspec_gb300_ingest_files(rawspec_context *ctx, const char *cons
     }
     rawspec_gb300_raw_hdr h;
     off_t pos = rawspec_gb300_raw_read_header(fd, &h);
-    while (pos > 0) {
+    while (pos > 0 && !lib_error) {
       if (h.obsnchan < schan + ctx->Nc || chan_bytes * h.obsnchan != h.blocsize) {
         fprintf(stderr, "%s: block geometry differs from the context\n", paths[f]);
         st->stop = -1;
@@ -356,33 +468,33 @@ RSG_EXPORT int rawspec_gb300_ingest_files(rawspec_context *ctx, const char *cons
         break;
       }
       if (act == RAWSPEC_GB300_PKT_END_FILE) break;  /* the rest of this file is skipped */
-      for (int64_t z = 0; z < nfill; ++z) {  /* missing blocks: zeros */
-        memset(ctx->h_blkbufs[bi % ctx->Nb_host], 0, block_bytes);
+      for (int64_t z = 0; z < nfill && !lib_error; ++z) {  /* missing blocks: zeros */
+        pool_read(&pool, -1, 0, (char *)ctx->h_blkbufs[bi % ctx->Nb_host], block_bytes);
         st->blocks_zero++;
-        RSG_BUFFER_DONE();
+        lib_error = buffer_done(ctx, bi, expand4, st);
         ++bi;
       }
-      /* the block's channels [schan, schan + Nc) */
-      if (lseek(fd, (off_t)(chan_bytes * schan), SEEK_CUR) < 0) {
+      if (lib_error) break;
+      /* the block's channels [schan, schan + Nc): one contiguous range */
+      if (pool_read(&pool, fd, pos + (off_t)(chan_bytes * schan), (char *)ctx->h_blkbufs[bi % ctx->Nb_host],
+                    block_bytes) != 0) {
+        fprintf(stderr, "%s: incomplete block at end of file\n", paths[f]);
         st->stop = -1;
         break;
       }
-      const ssize_t got = read_fully(fd, ctx->h_blkbufs[bi % ctx->Nb_host], block_bytes);
-      if (got < 0 || (size_t)got < block_bytes) {
-        fprintf(stderr, "%s: %s\n", paths[f], got < 0 ? strerror(errno) : "incomplete block at end of file");
-        st->stop = -1;
-        break;
-      }
-      lseek(fd, (off_t)(chan_bytes * (h.obsnchan - schan - ctx->Nc)), SEEK_CUR);
       st->blocks_read++;
-      RSG_BUFFER_DONE();
+      lib_error = buffer_done(ctx, bi, expand4, st);
       ++bi;
+      if (lseek(fd, pos + (off_t)h.blocsize, SEEK_SET) < 0) {
+        st->stop = -1;
+        break;
+      }
       pos = rawspec_gb300_raw_read_header(fd, &h);
     }
     if (pos < 0) fprintf(stderr, "%s: cannot read a block header\n", paths[f]);
     close(fd);
   }
-#undef RSG_BUFFER_DONE
-  if (rawspec_wait_for_completion(ctx) != 0) rc = 1;
-  return rc;
+  pool_stop(&pool);
+  if (rawspec_wait_for_completion(ctx) != 0) lib_error = 1;
+  return lib_error ? 1 : 0;
 }
