@@ -18,6 +18,10 @@ Metric: RAW-in GB/s (RAW bytes of the step / step time).
          percentiles of one loop iteration (the wait for the previous buffer
          and the copy and start of this one).
 
+ingest  GUPPI RAW files of the same shape in /dev/shm streamed through
+        rawspec_gb300_ingest_files into filterbank files (RAW file bytes over
+        wall clock).
+
 `--impl reference` times the CPU restatement of the same chain (the
 reference has no CPU implementation of its spectrometer; the OpenMP FP32
 port under oracle/ stands in) with all host threads, on the same metric.
