@@ -88,6 +88,33 @@ __device__ __forceinline__ uint32_t expand2(uint32_t b0, uint32_t b1) {
   return r0 | (i0 << 8) | (r1 << 16) | (i1 << 24);
 }
 
+// Four packed bytes -> eight int8 components (re, im, re, im, ...): both
+// nibbles of every byte at once, sign-extended as (x ^ 8) - 8 per byte, then
+// interleaved high (real) / low (imaginary).
+__device__ __forceinline__ uint2 expand_word(uint32_t w) {
+  const uint32_t hi = __vsub4(((w >> 4) & 0x0f0f0f0fu) ^ 0x08080808u, 0x08080808u);
+  const uint32_t lo = __vsub4((w & 0x0f0f0f0fu) ^ 0x08080808u, 0x08080808u);
+  return make_uint2(__byte_perm(hi, lo, 0x5140), __byte_perm(hi, lo, 0x7362));
+}
+
+// 16 packed bytes per thread; grid.y = (block, channel) segments of the
+// launch, grid.x covers one segment (blk_bytes_packed % 16 == 0).
+__global__ void k_expand4_vec(Expand4Launch a) {
+  const int seg = blockIdx.y;
+  const int c = a.c0 + seg % a.nch;
+  const int blk = (a.dst_block + seg / a.nch) % a.Nb;
+  const long long pin = (long long)c * a.Nb * a.blk_bytes_packed + (long long)blk * a.blk_bytes_packed;
+  const long long n16 = a.blk_bytes_packed / 16;
+  const uint4* src = reinterpret_cast<const uint4*>(a.packed + pin);
+  uint4* dst = reinterpret_cast<uint4*>(a.out + 2 * pin);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n16; i += (long long)gridDim.x * blockDim.x) {
+    const uint4 p = __ldg(src + i);
+    const uint2 e0 = expand_word(p.x), e1 = expand_word(p.y), e2 = expand_word(p.z), e3 = expand_word(p.w);
+    dst[2 * i] = make_uint4(e0.x, e0.y, e1.x, e1.y);
+    dst[2 * i + 1] = make_uint4(e2.x, e2.y, e3.x, e3.y);
+  }
+}
+
 __global__ void k_expand4_words(Expand4Launch a) {
   // one thread per 4 packed bytes; blk_bytes_packed % 4 == 0
   const long long words_per_seg = a.blk_bytes_packed / 4;
@@ -129,6 +156,15 @@ cudaError_t expand4_launch(const Expand4Launch& Lin, cudaStream_t s) {
   if (L.nch < 0) {
     L.c0 = 0;
     L.nch = L.Nc;
+  }
+  const long long nseg = (long long)L.nch * L.num_blocks;
+  if (L.blk_bytes_packed % 16 == 0 && nseg >= 1 && nseg <= 65535 &&
+      (reinterpret_cast<uintptr_t>(L.packed) & 15) == 0 && (reinterpret_cast<uintptr_t>(L.out) & 15) == 0) {
+    const long long n16 = L.blk_bytes_packed / 16;
+    const long long want = std::max<long long>(1, (152LL * 16 + nseg - 1) / nseg);  // ~16 CTAs per SM in all
+    const int gx = (int)std::max<long long>(1, std::min<long long>((n16 + 255) / 256, want));
+    k_expand4_vec<<<dim3(gx, (unsigned)nseg), 256, 0, s>>>(L);
+    return cudaGetLastError();
   }
   const bool words = (L.blk_bytes_packed % 4) == 0;
   const long long items = (words ? L.blk_bytes_packed / 4 : L.blk_bytes_packed) * L.nch * L.num_blocks;
