@@ -69,6 +69,7 @@ struct Product {
   int chunks = 1;
   bool fused = false;      // persistent fused four-step kernel
   int* d_ctl = nullptr;    // its control words
+  int* h_err = nullptr;    // pinned copy of the error word, refreshed after every fused launch
   float* d_partial = nullptr;  // per-chunk partial sums of this product
   float2* d_scratch = nullptr; // four-step intermediate (or the fused kernel's ring)
   cudaStream_t own_stream = nullptr;  // the product's kernels run concurrently with the others'
@@ -418,9 +419,14 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
     L.unit0 = c0 * L.units_per_chan;
     L.unit_count = (c1 - c0) * L.units_per_chan;
     if (P.fused) {
-      ProfScope ps(g, RAWSPEC_GB300_K_LARGE_FUSED, P.stream);
-      RSG_CUDA(large_fused_launch(L, P.stream));
-      g->launches++;
+      {
+        ProfScope ps(g, RAWSPEC_GB300_K_LARGE_FUSED, P.stream);
+        RSG_CUDA(large_fused_launch(L, P.stream));
+        g->launches++;
+      }
+      // the error word follows the launch to the host, so that a wait needs no
+      // synchronous copy
+      RSG_CUDA(cudaMemcpyAsync(P.h_err, P.d_ctl, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
       return 0;
     }
     {
@@ -706,6 +712,8 @@ int rawspec_initialize(rawspec_context* ctx) {
         const size_t nctl = (size_t)large_fused_ctl_ints(L);
         if (dev_alloc(g, &P.d_ctl, nctl * sizeof(int))) FAIL();
         CK(cudaMemsetAsync(P.d_ctl, 0, nctl * sizeof(int), g->stream));
+        CK(cudaHostAlloc((void**)&P.h_err, sizeof(int), cudaHostAllocDefault));
+        *P.h_err = 0;
         L.ctl = P.d_ctl;
       }
       if (sf && dev_alloc(g, &P.d_scratch, sf * sizeof(float2))) FAIL();
@@ -781,6 +789,7 @@ void rawspec_cleanup(rawspec_context* ctx) {
     cudaFree(g->prod[i].d_ics);
     cudaFree(g->prod[i].d_tw);
     cudaFree(g->prod[i].d_ctl);
+    if (g->prod[i].h_err) cudaFreeHost(g->prod[i].h_err);
     cudaFree(g->prod[i].d_partial);
     cudaFree(g->prod[i].d_scratch);
     if (g->prod[i].own_stream) {
@@ -963,9 +972,8 @@ int rawspec_wait_for_completion(rawspec_context* ctx) {
     for (unsigned i = 0; i < ctx->No; i++) RSG_CUDA(cudaLaunchHostFunc(g->stream, pre_dump_fn, &g->cb[i]));
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) return 1;
   for (unsigned i = 0; i < ctx->No; i++) {
-    if (!g->prod[i].d_ctl) continue;
-    int err = 0;
-    if (cudaMemcpy(&err, g->prod[i].d_ctl, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    if (!g->prod[i].h_err) continue;
+    const int err = *g->prod[i].h_err;  // copied behind every fused launch, ordered before the join
     if (err) {
       fprintf(stderr, "rawspec: product %u: a bounded wait of the fused FFT kernel timed out (code %d: 1 ring slot, "
                       "2 column tiles, 3 stage copy)\n", i, err);
