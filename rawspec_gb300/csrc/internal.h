@@ -105,7 +105,7 @@ struct LargeLaunch {
   int unit0 = 0, unit_count = 0;  // units of this launch (two-kernel path)
   int ring = 0;                   // intermediate slots
   int lag = 2;                    // row tiles of slab s follow the column tiles of slab s + lag
-  int* ctl = nullptr;             // [0] error, [1] item counter, [2..2+S) A done, [2+S..2+2S) B done
+  int* ctl = nullptr;             // [0] error, [1] CTAs finished, [2] item counter, [3..3+S) A done, [3+S..3+2S) B done
   int fused_ctas = 0;             // persistent grid size
   // fused kernel: tensor maps of the input (rows of N1 words), of the
   // twiddle tables twJ and twM and of the dump buffer (rows of N2 floats)
@@ -129,7 +129,7 @@ cudaError_t large_prepare(const LargeLaunch& L);
 // spectrum.  large_fused_plan() sets the grid size, the lag and the number of
 // intermediate slabs (ring); the launch needs ring * 2 * N float2 of scratch
 // and large_fused_ctl_ints() control words (zeroed once before the first
-// launch).
+// launch; each launch leaves them zeroed for the next, the error word apart).
 bool large_fused_supported(const LargeLaunch& L);
 cudaError_t large_fused_plan(LargeLaunch& L);
 int large_fused_row_radix(int pol);  // radix of the row tiles (twiddle table of twN1)

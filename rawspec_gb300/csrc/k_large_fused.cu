@@ -329,9 +329,10 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
   constexpr int itemsA = tilesA / K, itemsB = tilesB / K;
   const long long total = (long long)S * (itemsA + itemsB);
   int* err = a.ctl;  // sticky error word (never reset by a launch)
-  int* next = a.ctl + 1;
-  int* doneA = a.ctl + 2;
-  int* doneB = a.ctl + 2 + S;
+  int* exited = a.ctl + 1;  // CTAs of this launch that have finished
+  int* next = a.ctl + 2;
+  int* doneA = a.ctl + 3;
+  int* doneB = a.ctl + 3 + S;
   const float im_sign = a.conj ? -1.0f : 1.0f;
   const unsigned long long pol_first = policy_evict_first();
   const unsigned long long pol_last = policy_evict_last();
@@ -603,6 +604,21 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
   }
   // output copies still in flight complete before the CTA retires
   if (TOUT && tid == 0) bulk_wait_all();
+  // The last CTA to finish zeroes the counters for the next launch (every
+  // other CTA has stopped reading them); the error word stays.
+  __shared__ int s_last;
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    s_last = atomicAdd(exited, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    for (int i = tid; i < 1 + 2 * S; i += kFusedTPB) next[i] = 0;
+    if (tid == 0) *exited = 0;
+    __threadfence();
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -723,7 +739,7 @@ int large_fused_row_radix(int pol) { return pol == POL_TP ? fused_rb<POL_TP>() :
 
 int large_fused_col_radix() { return fused_ra(); }
 
-int large_fused_ctl_ints(const LargeLaunch& L) { return 2 + 2 * L.Nc * L.Nss; }
+int large_fused_ctl_ints(const LargeLaunch& L) { return 3 + 2 * L.Nc * L.Nss; }
 
 namespace {
 
@@ -779,9 +795,8 @@ cudaError_t large_fused_prepare(LargeLaunch& L) {
 }
 
 cudaError_t large_fused_launch(const LargeLaunch& L, cudaStream_t s) {
-  // reset the item counter and the per-slab counters; ctl[0] keeps errors
-  cudaError_t e = cudaMemsetAsync(L.ctl + 1, 0, sizeof(int) * (size_t)(large_fused_ctl_ints(L) - 1), s);
-  if (e != cudaSuccess) return e;
+  // the counters were zeroed at initialisation and are zeroed again by the
+  // last CTA of every launch
   return fused_dispatch(L, s, 0, nullptr);
 }
 
