@@ -206,7 +206,7 @@ def cpu_baseline_leg(min_seconds: float = 12.0) -> dict:
                       f"total power, {secs:.1f} s"}
 
 
-def ingest_leg(nbuf: int = 4) -> dict:
+def ingest_leg(nbuf: int = 8) -> dict:
     """GUPPI RAW files -> librawspec -> SIGPROC filterbank files at the
     production shape: a two-file stem of 2 * nbuf blocks (128 MiB each) in
     /dev/shm (RAM-backed), streamed by rawspec_gb300_ingest_files with the
@@ -254,10 +254,14 @@ def ingest_leg(nbuf: int = 4) -> dict:
             ctx.dump_callback = Cc.cast(L.rawspec_gb300_fil_dump_callback, api.DUMP_CALLBACK)
             plist = (Cc.c_char_p * 2)(*[str(p).encode() for p in paths])
             st = io.IngestStats()
-            L.rawspec_gb300_ingest_files(Cc.byref(ctx), plist, 2, 0, 0, Cc.byref(st))  # warm-up (page cache, GPU)
+            ing = L.rawspec_gb300_ingest_open(Cc.byref(ctx), 0)
+            if not ing:
+                raise RuntimeError("ingest open")
+            L.rawspec_gb300_ingest_stem(ing, plist, 2, 0, Cc.byref(st))  # warm-up (page cache, GPU)
             t0 = time.perf_counter()
-            rc = L.rawspec_gb300_ingest_files(Cc.byref(ctx), plist, 2, 0, 0, Cc.byref(st))
+            rc = L.rawspec_gb300_ingest_stem(ing, plist, 2, 0, Cc.byref(st))
             dt = time.perf_counter() - t0
+            L.rawspec_gb300_ingest_close(ing)
             if rc != 0 or st.stop != 0:
                 raise RuntimeError("ingest failed")
         finally:
@@ -267,7 +271,7 @@ def ingest_leg(nbuf: int = 4) -> dict:
         file_bytes = sum(p.stat().st_size for p in paths)
     return {"value": file_bytes / dt / 1e9, "unit": "GB/s", "files": 2, "file_bytes": file_bytes,
             "blocks": int(st.blocks_read), "buffers": int(st.buffers), "storage": str(base),
-            "timing": "wall clock of rawspec_gb300_ingest_files over the stem (warm page cache), filterbank "
+            "timing": "wall clock of rawspec_gb300_ingest_stem over the stem (warm page cache), filterbank "
                       "files written by the dump callback"}
 
 

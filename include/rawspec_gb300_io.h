@@ -115,6 +115,18 @@ typedef struct {
 int rawspec_gb300_ingest_files(rawspec_context *ctx, const char *const *paths, int npaths, unsigned int schan,
                                int expand4, rawspec_gb300_ingest_stats *stats);
 
+/* The same as a reusable handle, for a context that streams several stems:
+ * open allocates a second set of pinned host blocks (the file reads of one
+ * buffer overlap the host-to-device copy of the previous one, the context's
+ * block pointers being switched per buffer and restored at the end of each
+ * stem) and the reader threads; NULL on failure.  rawspec_gb300_ingest_files
+ * is open + stem + close. */
+typedef struct rawspec_gb300_ingest rawspec_gb300_ingest;
+rawspec_gb300_ingest *rawspec_gb300_ingest_open(rawspec_context *ctx, int expand4);
+int rawspec_gb300_ingest_stem(rawspec_gb300_ingest *ingest, const char *const *paths, int npaths, unsigned int schan,
+                              rawspec_gb300_ingest_stats *stats);
+void rawspec_gb300_ingest_close(rawspec_gb300_ingest *ingest);
+
 /* ---------------------------------------------------------------------------
  * SIGPROC filterbank output
  * ------------------------------------------------------------------------- */

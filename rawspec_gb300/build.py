@@ -61,8 +61,9 @@ def _extra_flags() -> list[str]:
 def _compile(src: Path, verbose: bool) -> Path:
     obj = BUILD / (src.stem + src.suffix.replace(".", "_") + ".o")
     if src.suffix == ".c":
+        cuda_inc = Path(nvcc()).resolve().parent.parent / "include"  # the runtime API header
         cmd = [os.environ.get("CC", "gcc"), "-std=gnu11", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall",
-               f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)]
+               f"-I{INCLUDE}", f"-I{CSRC}", f"-I{cuda_inc}", "-c", str(src), "-o", str(obj)]
     else:
         cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *_extra_flags(), "-c", str(src), "-o", str(obj)]
     if verbose:

@@ -20,6 +20,8 @@
 #include <string.h>
 #include <unistd.h>
 
+#include <cuda_runtime_api.h>
+
 #include "rawspec_gb300_io.h"
 
 #define RSG_EXPORT __attribute__((visibility("default")))
@@ -416,85 +418,239 @@ static int pool_read(ReaderPool *p, int fd, off_t off, char *dst, size_t bytes) 
   return 0;
 }
 
-/* Hands the host blocks to the GPU once block bi completes a buffer. */
-static int buffer_done(rawspec_context *ctx, long long bi, int expand4, rawspec_gb300_ingest_stats *st) {
-  if (bi % ctx->Nb != ctx->Nb - 1) return 0;
-  if (rawspec_wait_for_completion(ctx) != 0) return 1;
-  if (rawspec_copy_blocks_to_gpu_and_start_processing(ctx, ctx->Nb, (char)(expand4 ? 1 : 0), RAWSPEC_FORWARD_FFT) != 0)
-    return 1;
-  st->buffers++;
-  return 0;
+/* ---------------------------------------------------------------------------
+ * The stem's blocks are read on a reader thread into one of two sets of
+ * pinned host blocks while the calling thread hands the other set to the GPU
+ * (wait_for_completion + copy_blocks_to_gpu_and_start_processing, with the
+ * context's block pointers switched to that set), so that file reads
+ * overlap the host-to-device copies.  The context's own blocks are the first
+ * set and are restored at the end; the second set is allocated here.  Only
+ * the calling thread calls the library.
+ * ------------------------------------------------------------------------- */
+#define RSG_MAX_NB 64
+
+typedef struct {
+  /* fixed */
+  rawspec_context *ctx;
+  const char *const *paths;
+  int npaths;
+  unsigned schan;
+  size_t chan_bytes, block_bytes;
+  char *sets[2][RSG_MAX_NB];
+  ReaderPool *pool;
+  /* hand-off */
+  pthread_mutex_t mu;
+  pthread_cond_t cv;
+  int filled[2];   /* a full buffer waits in the set */
+  int busy[2];     /* the set is being filled or handed over */
+  int reader_done;
+  int abort;
+  /* results (reader) */
+  long long blocks_read, blocks_zero;
+  int stop;
+} Ingest;
+
+/* Reader: claims set k (waits while the GPU side still uses it). */
+static int claim_set(Ingest *in, int k) {
+  pthread_mutex_lock(&in->mu);
+  while ((in->filled[k] || in->busy[k]) && !in->abort) pthread_cond_wait(&in->cv, &in->mu);
+  const int ok = !in->abort;
+  if (ok) in->busy[k] = 1;
+  pthread_mutex_unlock(&in->mu);
+  return ok;
 }
 
-RSG_EXPORT int rawspec_gb300_ingest_files(rawspec_context *ctx, const char *const *paths, int npaths, unsigned int schan,
-                                          int expand4, rawspec_gb300_ingest_stats *st) {
-  rawspec_gb300_ingest_stats local;
-  if (!st) st = &local;
-  memset(st, 0, sizeof(*st));
-  if (!ctx || !ctx->h_blkbufs || ctx->Nb == 0 || ctx->Nb_host == 0) return 1;
-  /* bytes of one channel of one block in the file and in a host block */
-  const size_t file_bits = expand4 ? 4 : ctx->Nbps;
-  const size_t chan_bytes = (size_t)2 * ctx->Np * file_bits / 8 * ctx->Ntpb;
-  const size_t block_bytes = chan_bytes * ctx->Nc;
+static void publish_set(Ingest *in, int k) {
+  pthread_mutex_lock(&in->mu);
+  in->busy[k] = 0;
+  in->filled[k] = 1;
+  pthread_cond_broadcast(&in->cv);
+  pthread_mutex_unlock(&in->mu);
+}
+
+static void *ingest_reader(void *arg) {
+  Ingest *in = (Ingest *)arg;
+  rawspec_context *ctx = in->ctx;
   rawspec_gb300_pktidx_state ps;
   memset(&ps, 0, sizeof(ps));
   long long bi = 0;  /* block index across the stem */
-  int lib_error = 0;
-  ReaderPool pool;
-  ReaderArg args[RSG_MAX_READERS];
-  pool_start(&pool, args);
-
-  for (int f = 0; f < npaths && st->stop == 0 && !lib_error; ++f) {
-    const int fd = open(paths[f], O_RDONLY);
+  int set = 0;
+  int have = claim_set(in, 0);
+  for (int f = 0; f < in->npaths && in->stop == 0 && have; ++f) {
+    const int fd = open(in->paths[f], O_RDONLY);
     if (fd < 0) {
-      fprintf(stderr, "cannot open %s: %s\n", paths[f], strerror(errno));
-      st->stop = -1;
+      fprintf(stderr, "cannot open %s: %s\n", in->paths[f], strerror(errno));
+      in->stop = -1;
       break;
     }
     rawspec_gb300_raw_hdr h;
     off_t pos = rawspec_gb300_raw_read_header(fd, &h);
-    while (pos > 0 && !lib_error) {
-      if (h.obsnchan < schan + ctx->Nc || chan_bytes * h.obsnchan != h.blocsize) {
-        fprintf(stderr, "%s: block geometry differs from the context\n", paths[f]);
-        st->stop = -1;
+    while (pos > 0 && have) {
+      if (h.obsnchan < in->schan + ctx->Nc || in->chan_bytes * h.obsnchan != h.blocsize) {
+        fprintf(stderr, "%s: block geometry differs from the context\n", in->paths[f]);
+        in->stop = -1;
         break;
       }
       int64_t nfill = 0;
       const int act = rawspec_gb300_pktidx_step(&ps, h.pktidx, &nfill);
       if (act == RAWSPEC_GB300_PKT_BACKWARD || act == RAWSPEC_GB300_PKT_MISALIGNED) {
-        fprintf(stderr, "%s: %s jump in pktidx to %lld\n", paths[f],
+        fprintf(stderr, "%s: %s jump in pktidx to %lld\n", in->paths[f],
                 act == RAWSPEC_GB300_PKT_BACKWARD ? "backwards" : "misaligned", (long long)h.pktidx);
-        st->stop = act;
+        in->stop = act;
         break;
       }
       if (act == RAWSPEC_GB300_PKT_END_FILE) break;  /* the rest of this file is skipped */
-      for (int64_t z = 0; z < nfill && !lib_error; ++z) {  /* missing blocks: zeros */
-        pool_read(&pool, -1, 0, (char *)ctx->h_blkbufs[bi % ctx->Nb_host], block_bytes);
-        st->blocks_zero++;
-        lib_error = buffer_done(ctx, bi, expand4, st);
+      /* missing blocks (zeros), then the block's channels [schan, schan + Nc) */
+      for (int64_t z = 0; z <= nfill && have; ++z) {
+        char *dst = in->sets[set][bi % ctx->Nb];
+        if (z < nfill) {
+          pool_read(in->pool, -1, 0, dst, in->block_bytes);
+          in->blocks_zero++;
+        } else {
+          if (pool_read(in->pool, fd, pos + (off_t)(in->chan_bytes * in->schan), dst, in->block_bytes) != 0) {
+            fprintf(stderr, "%s: incomplete block at end of file\n", in->paths[f]);
+            in->stop = -1;
+            break;
+          }
+          in->blocks_read++;
+        }
+        if (bi % ctx->Nb == ctx->Nb - 1) {  /* a full buffer: hand it over, go on in the other set */
+          publish_set(in, set);
+          set ^= 1;
+          have = claim_set(in, set);
+        }
         ++bi;
       }
-      if (lib_error) break;
-      /* the block's channels [schan, schan + Nc): one contiguous range */
-      if (pool_read(&pool, fd, pos + (off_t)(chan_bytes * schan), (char *)ctx->h_blkbufs[bi % ctx->Nb_host],
-                    block_bytes) != 0) {
-        fprintf(stderr, "%s: incomplete block at end of file\n", paths[f]);
-        st->stop = -1;
-        break;
-      }
-      st->blocks_read++;
-      lib_error = buffer_done(ctx, bi, expand4, st);
-      ++bi;
+      if (in->stop) break;
       if (lseek(fd, pos + (off_t)h.blocsize, SEEK_SET) < 0) {
-        st->stop = -1;
+        in->stop = -1;
         break;
       }
       pos = rawspec_gb300_raw_read_header(fd, &h);
     }
-    if (pos < 0) fprintf(stderr, "%s: cannot read a block header\n", paths[f]);
+    if (pos < 0) fprintf(stderr, "%s: cannot read a block header\n", in->paths[f]);
     close(fd);
   }
-  pool_stop(&pool);
+  pthread_mutex_lock(&in->mu);
+  if (have) in->busy[set] = 0;  /* a partial buffer is dropped */
+  in->reader_done = 1;
+  pthread_cond_broadcast(&in->cv);
+  pthread_mutex_unlock(&in->mu);
+  return NULL;
+}
+
+/* The reusable part of an ingest: the second set of host blocks and the
+ * reader pool. */
+struct rawspec_gb300_ingest {
+  rawspec_context *ctx;
+  int expand4;
+  size_t chan_bytes, block_bytes;
+  char *second[RSG_MAX_NB];
+  ReaderPool pool;
+  ReaderArg args[RSG_MAX_READERS];
+};
+
+RSG_EXPORT rawspec_gb300_ingest *rawspec_gb300_ingest_open(rawspec_context *ctx, int expand4) {
+  if (!ctx || !ctx->h_blkbufs || ctx->Nb == 0 || ctx->Nb > RSG_MAX_NB || ctx->Nb_host < ctx->Nb) return NULL;
+  rawspec_gb300_ingest *g = (rawspec_gb300_ingest *)calloc(1, sizeof(*g));
+  if (!g) return NULL;
+  g->ctx = ctx;
+  g->expand4 = expand4;
+  /* bytes of one channel of one block in the file and in a host block */
+  const size_t file_bits = expand4 ? 4 : ctx->Nbps;
+  g->chan_bytes = (size_t)2 * ctx->Np * file_bits / 8 * ctx->Ntpb;
+  g->block_bytes = g->chan_bytes * ctx->Nc;
+  for (unsigned b = 0; b < ctx->Nb; ++b)
+    if (cudaHostAlloc((void **)&g->second[b], g->block_bytes, cudaHostAllocPortable) != cudaSuccess) {
+      for (unsigned i = 0; i < b; ++i) cudaFreeHost(g->second[i]);
+      free(g);
+      return NULL;
+    }
+  pool_start(&g->pool, g->args);
+  return g;
+}
+
+RSG_EXPORT void rawspec_gb300_ingest_close(rawspec_gb300_ingest *g) {
+  if (!g) return;
+  pool_stop(&g->pool);
+  for (unsigned b = 0; b < g->ctx->Nb; ++b) cudaFreeHost(g->second[b]);
+  free(g);
+}
+
+RSG_EXPORT int rawspec_gb300_ingest_stem(rawspec_gb300_ingest *g, const char *const *paths, int npaths,
+                                         unsigned int schan, rawspec_gb300_ingest_stats *st) {
+  rawspec_gb300_ingest_stats local;
+  if (!st) st = &local;
+  memset(st, 0, sizeof(*st));
+  if (!g) return 1;
+  rawspec_context *ctx = g->ctx;
+  Ingest in;
+  memset(&in, 0, sizeof(in));
+  in.ctx = ctx;
+  in.paths = paths;
+  in.npaths = npaths;
+  in.schan = schan;
+  in.chan_bytes = g->chan_bytes;
+  in.block_bytes = g->block_bytes;
+  in.pool = &g->pool;
+  char *own[RSG_MAX_NB];
+  for (unsigned b = 0; b < ctx->Nb; ++b) {
+    own[b] = ctx->h_blkbufs[b];
+    in.sets[0][b] = own[b];
+    in.sets[1][b] = g->second[b];
+  }
+  int lib_error = 0;
+  pthread_mutex_init(&in.mu, NULL);
+  pthread_cond_init(&in.cv, NULL);
+  pthread_t reader;
+  if (pthread_create(&reader, NULL, ingest_reader, &in) != 0) {
+    fprintf(stderr, "rawspec_gb300_ingest_stem: cannot start the reader thread\n");
+    pthread_cond_destroy(&in.cv);
+    pthread_mutex_destroy(&in.mu);
+    return 1;
+  }
+  /* GPU side: hand over the filled sets in turn */
+  int k = 0;
+  for (;;) {
+    pthread_mutex_lock(&in.mu);
+    while (!in.filled[k] && !in.reader_done) pthread_cond_wait(&in.cv, &in.mu);
+    const int ready = in.filled[k];
+    pthread_mutex_unlock(&in.mu);
+    if (!ready) break;
+    for (unsigned b = 0; b < ctx->Nb; ++b) ctx->h_blkbufs[b] = in.sets[k][b];
+    if (rawspec_wait_for_completion(ctx) != 0 ||
+        rawspec_copy_blocks_to_gpu_and_start_processing(ctx, ctx->Nb, (char)(g->expand4 ? 1 : 0),
+                                                        RAWSPEC_FORWARD_FFT) != 0)
+      lib_error = 1;
+    else
+      st->buffers++;
+    pthread_mutex_lock(&in.mu);
+    in.filled[k] = 0;  /* the copy is done: the set may be refilled */
+    if (lib_error) in.abort = 1;
+    pthread_cond_broadcast(&in.cv);
+    pthread_mutex_unlock(&in.mu);
+    if (lib_error) break;
+    k ^= 1;
+  }
+  pthread_join(reader, NULL);
   if (rawspec_wait_for_completion(ctx) != 0) lib_error = 1;
+  for (unsigned b = 0; b < ctx->Nb; ++b) ctx->h_blkbufs[b] = own[b];
+  pthread_cond_destroy(&in.cv);
+  pthread_mutex_destroy(&in.mu);
+  st->blocks_read = in.blocks_read;
+  st->blocks_zero = in.blocks_zero;
+  st->stop = in.stop;
   return lib_error ? 1 : 0;
+}
+
+RSG_EXPORT int rawspec_gb300_ingest_files(rawspec_context *ctx, const char *const *paths, int npaths, unsigned int schan,
+                                          int expand4, rawspec_gb300_ingest_stats *st) {
+  rawspec_gb300_ingest *g = rawspec_gb300_ingest_open(ctx, expand4);
+  if (!g) {
+    if (st) memset(st, 0, sizeof(*st));
+    return 1;
+  }
+  const int rc = rawspec_gb300_ingest_stem(g, paths, npaths, schan, st);
+  rawspec_gb300_ingest_close(g);
+  return rc;
 }

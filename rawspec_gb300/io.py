@@ -87,6 +87,10 @@ def lib() -> C.CDLL:
                                                         C.POINTER(C.c_int)]),
             "rawspec_gb300_ingest_files": (C.c_int, [P, C.POINTER(C.c_char_p), C.c_int, C.c_uint, C.c_int,
                                                      C.POINTER(IngestStats)]),
+            "rawspec_gb300_ingest_open": (C.c_void_p, [P, C.c_int]),
+            "rawspec_gb300_ingest_stem": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.c_int, C.c_uint,
+                                                    C.POINTER(IngestStats)]),
+            "rawspec_gb300_ingest_close": (None, [C.c_void_p]),
             "rawspec_gb300_fil_header": (C.c_long, [C.POINTER(FilHeader), C.c_void_p, C.c_size_t]),
             "rawspec_gb300_telescope_id": (C.c_int, [C.c_char_p]),
             "rawspec_gb300_fil_header_for_product": (C.c_int, [C.POINTER(RawHeader), P, C.c_int, C.c_uint,
