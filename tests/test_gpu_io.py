@@ -91,3 +91,44 @@ def test_raw_stem_to_filterbank_files(cuda_device, tmp_path):
         got = np.frombuffer(raw[len(hdr):], dtype=np.float32)
         assert got.size == want[i].size
         np.testing.assert_array_equal(got, want[i])
+
+
+def test_ingest_handle_streams_several_stems(cuda_device, tmp_path):
+    # one handle, the same stem twice with the integration reset between:
+    # the second pass's dumps repeat the first's (both host-block sets are
+    # used, the context's own blocks are restored after each stem)
+    blocks = _blocks()
+    paths = []
+    for k, (a, b, dio) in enumerate(FILES):
+        p = tmp_path / f"stem.{k:04d}.raw"
+        io.write_raw_file(p, [blocks[i].view(np.uint8).reshape(-1) for i in range(a, b)], PKTIDX[a:b], OBSNCHAN, NP,
+                          NBITS, NTPB, directio=dio)
+        paths.append(p)
+    L = io.lib()
+    first = io.RawHeader()
+    fd = os.open(paths[0], os.O_RDONLY)
+    assert L.rawspec_gb300_raw_read_header(fd, C.byref(first)) > 0
+    os.close(fd)
+    spec = api.Spectrometer(NCHAN, NP, NTPB, 8, PRODUCTS, conj=1)  # collects the dumps
+    try:
+        own = [spec.ctx.h_blkbufs[b] for b in range(spec.ctx.Nb)]
+        ing = L.rawspec_gb300_ingest_open(C.byref(spec.ctx), 0)
+        assert ing
+        plist = (C.c_char_p * len(paths))(*[str(p).encode() for p in paths])
+        st = io.IngestStats()
+        try:
+            assert L.rawspec_gb300_ingest_stem(ing, plist, len(paths), SCHAN, C.byref(st)) == 0
+            n1 = [len(d) for d in spec.dumps]
+            assert L.rawspec_reset_integration(C.byref(spec.ctx)) == 0
+            assert L.rawspec_gb300_ingest_stem(ing, plist, len(paths), SCHAN, C.byref(st)) == 0
+        finally:
+            L.rawspec_gb300_ingest_close(ing)
+        assert [spec.ctx.h_blkbufs[b] for b in range(spec.ctx.Nb)] == own
+        assert (st.blocks_read, st.blocks_zero, st.buffers) == (5, 1, 3)
+        for i in range(len(PRODUCTS)):
+            d = [np.asarray(x) for x in spec.dumps[i]]
+            assert len(d) == 2 * n1[i]
+            for a, b in zip(d[:n1[i]], d[n1[i]:]):
+                np.testing.assert_array_equal(a, b)
+    finally:
+        spec.close()
