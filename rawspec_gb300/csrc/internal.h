@@ -75,6 +75,36 @@ struct FinalizeLaunch {
 cudaError_t finalize_launch(const FinalizeLaunch& L, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
+// Tensor-core DFT product kernel (k_tc.cu): N = S * S with S = 16, 32, 64,
+// 8-bit input of two polarisations, units of a multiple of 64 / S spectra.
+// Units, chunks, partial sums and outputs as in SmallLaunch.
+// ---------------------------------------------------------------------------
+struct TcLaunch {
+  int logN = 0, pol = POL_TP;
+  int Nc = 0, M = 0, units_per_chan = 0, n_units = 0;
+  long long chan_stride = 0;     // samples per channel in the device buffer
+  const void* in = nullptr;
+  float* out = nullptr;          // [units_per_chan][|P|][Nc][N], FFT-shifted
+  float* partial = nullptr;      // [n_units][chunks][|P|][N] (chunks > 1)
+  const void* tab = nullptr;     // tc_table_bytes(logN) bytes from tc_table_fill
+  int* err = nullptr;            // set to 1 if a bounded wait for the tensor cores timed out
+  int mode = ACC_WRITE, inverse = 0, conj = 0;
+  float scale = 1.0f;
+  int unit0 = 0, unit_count = 0;
+  int chunks = 1, spc = 0;       // chunks per unit, spectra per chunk (whole buffer)
+  int chunks_pipe = 1, spc_pipe = 0;  // the same for a launch over one channel group
+  int slots = 0;                 // resident CTAs on the device (the grid size cap)
+  size_t smem = 0;
+};
+bool tc_supported(int logN, int fmt, int nv, int pol, int M);
+size_t tc_table_bytes(int logN);
+cudaError_t tc_table_fill(void* dst, int logN, cudaStream_t s);
+// Sets the dynamic shared-memory limit, the grid cap and the chunking;
+// partial_floats receives the scratch the launches need.  0, or -1.
+int tc_configure(TcLaunch& L, size_t* partial_floats, int pipe_groups);
+cudaError_t tc_launch(const TcLaunch& L, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
 // Four-step large FFT (4096 < N <= 2^22): N = N1 * N2.
 //   pass A: N2-point FFTs down the columns n1 of x[n1 + N1*n2], twiddled by
 //           W_N^(n1*k2), written to scratch as [slab][pol][k2][n1];

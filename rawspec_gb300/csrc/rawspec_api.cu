@@ -66,10 +66,12 @@ struct Product {
   float2* d_tw = nullptr;  // small: Stockham table; large: A table | B table | lo | hi | pass-A output twiddles
   SmallLaunch sl;
   LargeLaunch ll;
+  TcLaunch tl;
   int chunks = 1;
   bool fused = false;      // persistent fused four-step kernel
-  int* d_ctl = nullptr;    // its control words
-  int* h_err = nullptr;    // pinned copy of the error word, refreshed after every fused launch
+  bool tc = false;         // tensor-core DFT kernel instead of k_small
+  int* d_ctl = nullptr;    // control words of the fused kernel (error word first) or the tc error word
+  int* h_err = nullptr;    // pinned copy of the error word, refreshed after every fused or tc launch
   float* d_partial = nullptr;  // per-chunk partial sums of this product
   float2* d_scratch = nullptr; // four-step intermediate (or the fused kernel's ring)
   cudaStream_t own_stream = nullptr;  // the product's kernels run concurrently with the others'
@@ -175,6 +177,13 @@ void collect_profile(GpuCtx* g) {
 // ----------------------------------------------------------------------------
 bool is_pow2(unsigned x) { return x && !(x & (x - 1)); }
 int ilog2u(unsigned x) { int l = 0; while ((1u << l) < x) ++l; return l; }
+
+// Products of 8-bit input with N = 256, 1024 or 4096 run their DFT on the
+// tensor cores (k_tc) when RAWSPEC_GB300_TENSOR_DFT=1 at initialisation.
+bool tensor_dft_enabled() {
+  const char* v = getenv("RAWSPEC_GB300_TENSOR_DFT");
+  return v && v[0] == '1';
+}
 
 int validate_impl(rawspec_context* ctx, bool* expanded) {
   if (ctx->No == 0 || ctx->No > MAX_OUTPUTS) {
@@ -392,6 +401,27 @@ int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int unit0
 // Queues product i's kernels for the channels [c0, c1) of the buffer.
 int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse, int c0, int c1) {
   Product& P = g->prod[i];
+  if (P.tc) {
+    TcLaunch L = P.tl;
+    L.mode = mode;
+    L.inverse = inverse;
+    L.unit0 = c0 * L.units_per_chan;
+    L.unit_count = (c1 - c0) * L.units_per_chan;
+    if (c1 - c0 < (int)ctx->Nc) {  // a channel group: the finer split
+      L.chunks = L.chunks_pipe;
+      L.spc = L.spc_pipe;
+    }
+    {
+      ProfScope ps(g, RAWSPEC_GB300_K_TC, P.stream);
+      RSG_CUDA(tc_launch(L, P.stream));
+      g->launches++;
+    }
+    if (L.chunks > 1 &&
+        launch_finalize(ctx, g, P, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+      return 1;
+    RSG_CUDA(cudaMemcpyAsync(P.h_err, P.d_ctl, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
+    return 0;
+  }
   if (!P.large) {
     SmallLaunch L = P.sl;
     L.mode = mode;
@@ -655,7 +685,36 @@ int rawspec_initialize(rawspec_context* ctx) {
     }
 
     P.large = P.logN > 12;
-    if (!P.large) {
+    P.tc = !P.large && tensor_dft_enabled() && tc_supported(P.logN, g->fmt, (int)ctx->Np, pol, M);
+    if (P.tc) {
+      TcLaunch& L = P.tl;
+      L.logN = P.logN;
+      L.pol = pol;
+      L.Nc = (int)ctx->Nc;
+      L.M = M;
+      L.units_per_chan = upc;
+      L.n_units = (int)ctx->Nc * upc;
+      L.chan_stride = (long long)ctx->Nb * ctx->Ntpb;
+      L.in = g->d_in;
+      L.out = P.d_out;
+      L.conj = ctx->input_conjugated ? 1 : 0;
+      L.scale = scale;
+      size_t pf = 0;
+      if (tc_configure(L, &pf, std::min<int>(kMaxCopyGroups, (int)ctx->Nc))) {
+        fprintf(stderr, "tensor-core DFT kernel unavailable for FFT length %d\n", P.N);
+        FAIL();
+      }
+      if (pf && dev_alloc(g, &P.d_partial, pf * sizeof(float))) FAIL();
+      const size_t tb = tc_table_bytes(P.logN);
+      if (dev_alloc(g, &P.d_tw, (tb + 15) & ~size_t(15))) FAIL();
+      CK(tc_table_fill(P.d_tw, P.logN, g->stream));
+      L.tab = P.d_tw;
+      if (dev_alloc(g, &P.d_ctl, sizeof(int))) FAIL();
+      CK(cudaMemsetAsync(P.d_ctl, 0, sizeof(int), g->stream));
+      CK(cudaHostAlloc((void**)&P.h_err, sizeof(int), cudaHostAllocDefault));
+      *P.h_err = 0;
+      L.err = P.d_ctl;
+    } else if (!P.large) {
       SmallLaunch& L = P.sl;
       L.logN = P.logN;
       L.fmt = g->fmt;
@@ -748,6 +807,7 @@ int rawspec_initialize(rawspec_context* ctx) {
     }
   }
   for (unsigned i = 0; i < ctx->No; i++) {
+    g->prod[i].tl.partial = g->prod[i].d_partial;
     g->prod[i].sl.partial = g->prod[i].d_partial;
     g->prod[i].ll.partial = g->prod[i].d_partial;
     g->prod[i].ll.scratch = g->prod[i].d_scratch;
@@ -973,10 +1033,13 @@ int rawspec_wait_for_completion(rawspec_context* ctx) {
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) return 1;
   for (unsigned i = 0; i < ctx->No; i++) {
     if (!g->prod[i].h_err) continue;
-    const int err = *g->prod[i].h_err;  // copied behind every fused launch, ordered before the join
+    const int err = *g->prod[i].h_err;  // copied behind every fused or tc launch, ordered before the join
     if (err) {
-      fprintf(stderr, "rawspec: product %u: a bounded wait of the fused FFT kernel timed out (code %d: 1 ring slot, "
-                      "2 column tiles, 3 stage copy)\n", i, err);
+      if (g->prod[i].tc)
+        fprintf(stderr, "rawspec: product %u: a bounded wait for the tensor cores timed out\n", i);
+      else
+        fprintf(stderr, "rawspec: product %u: a bounded wait of the fused FFT kernel timed out (code %d: 1 ring "
+                        "slot, 2 column tiles, 3 stage copy)\n", i, err);
       return 1;
     }
   }
