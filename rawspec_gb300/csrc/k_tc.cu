@@ -50,12 +50,13 @@ struct TcCfg {
   static constexpr int B_BYTES = (ND / 8) * SBO;
   static constexpr int TW_BYTES = N * 8;      // W_N^(n2 k1) as [k1][n2] float2
   static constexpr int TAB_BYTES = B_BYTES + TW_BYTES;
-  static constexpr int SMEM = 2 * A_BYTES + TAB_BYTES + 32;  // + mbarrier and tensor-memory slot
-  static constexpr int TMEM_COLS = ND < 32 ? 32 : ND;
-  static constexpr int MINB = S == 16 ? 4 : S == 32 ? 3 : 1;
+  // stage-1 operand | T hi | T lo | DFT operand | twiddles | 2 mbarriers, tensor-memory slot
+  static constexpr int SMEM = 3 * A_BYTES + TAB_BYTES + 32;
+  static constexpr int TMEM_COLS = 2 * ND;    // stage-1 and stage-2 accumulators
+  static constexpr int MINB = 512 / TMEM_COLS;
   static constexpr int WPT = S / 2;           // input words per thread per tile
   static_assert(SPT * S == 64, "64 (spectrum, n2) pairs per tile, two threads each");
-  static_assert(NSEQ * (int)sizeof(float) * N <= 2 * A_BYTES, "reduction fits the operand area");
+  static_assert(4 * SPT * (int)sizeof(float) * N <= 3 * A_BYTES, "reduction fits the operand area");
 };
 
 namespace {
@@ -74,21 +75,29 @@ __device__ __forceinline__ uint32_t codes_to_h2(uint32_t x, uint32_t sel) {
 
 }  // namespace
 
+// Two tiles are in flight per CTA: the stage-1 MMAs of tile t+1 run while
+// tile t is detected, and the stage-2 MMAs of tile t+1 while the codes of
+// tile t+2 are converted.  Each accumulator (stage 1, stage 2) has its own
+// tensor-memory columns and its own mbarrier; every shared-memory operand is
+// rewritten only after the MMAs reading it have completed.
 template <int S, int POL>
 __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constant__ TcLaunch a) {
   using C = TcCfg<S>;
   constexpr int N = C::N, NSEQ = C::NSEQ, SPT = C::SPT, NP = PolOut<POL>::NP;
   constexpr int NACC = POL == POL_TP ? S : 2 * S;
-  constexpr uint32_t IDESC = tc::idesc_f16_f32(128, C::ND);
+  constexpr uint32_t IDESC = tc::idesc_f16_f32(128, C::ND);      // against [F hi | F lo]
+  constexpr uint32_t IDESC_HI = tc::idesc_f16_f32(128, C::ND / 2);  // against F hi alone
   static_assert(POL == POL_TP || S <= 32, "cross-pol modes keep 2 S accumulators per thread");
   extern __shared__ __align__(128) unsigned char sm[];
-  unsigned char* sAhi = sm;                  // stage-1 operand, then T hi
-  unsigned char* sAlo = sm + C::A_BYTES;     // T lo
-  unsigned char* sB = sm + 2 * C::A_BYTES;   // DFT matrix [hi | lo], then the twiddles
+  unsigned char* sA1 = sm;                   // stage-1 operand (integer codes)
+  unsigned char* sAhi = sm + C::A_BYTES;     // T hi
+  unsigned char* sAlo = sm + 2 * C::A_BYTES; // T lo
+  unsigned char* sB = sm + 3 * C::A_BYTES;   // DFT operand [hi | lo], then the twiddles
   const float2* sTw = reinterpret_cast<const float2*>(sB + C::B_BYTES);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(sB + C::TAB_BYTES);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
-  float* red = reinterpret_cast<float*>(sm);  // reduction area over both operands
+  uint64_t* mb1 = reinterpret_cast<uint64_t*>(sB + C::TAB_BYTES);
+  uint64_t* mb2 = mb1 + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mb1 + 2);
+  float* red = reinterpret_cast<float*>(sm);  // reduction area over the operands
 
   const int tid = threadIdx.x, warp = tid >> 5;
   {
@@ -96,7 +105,10 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
     uint4* dst = reinterpret_cast<uint4*>(sB);
     for (int i = tid; i < C::TAB_BYTES / 16; i += 128) dst[i] = __ldg(src + i);
   }
-  if (tid == 0) tc::mbar_init(mbar, 1);
+  if (tid == 0) {
+    tc::mbar_init(mb1, 1);
+    tc::mbar_init(mb2, 1);
+  }
   if (warp == 0) {
     tc::tmem_alloc(tslot, C::TMEM_COLS);
     tc::tmem_relinquish();
@@ -105,9 +117,11 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lanes
-  const uint32_t aHi = tc::smem_u32(sAhi), aLo = tc::smem_u32(sAlo), bF = tc::smem_u32(sB);
-  unsigned phase = 0;
+  const uint32_t d1 = tmem, d2 = tmem + C::ND;                       // accumulator columns
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;             // this warp's lanes
+  const uint32_t aA1 = tc::smem_u32(sA1), aHi = tc::smem_u32(sAhi), aLo = tc::smem_u32(sAlo);
+  const uint32_t bF = tc::smem_u32(sB);
+  unsigned ph1 = 0, ph2 = 0;
   int bad = 0;  // one of this thread's waits timed out
 
   // input words: thread -> (spectrum of the tile, n2), half of the n1 range
@@ -117,8 +131,142 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
   const int seq = tid / S, r = tid % S;
   const float im_sign = a.conj ? -1.0f : 1.0f;
 
+  uint32_t w[C::WPT];
+  auto load = [&](const uint32_t* p) {
+#pragma unroll
+    for (int j = 0; j < C::WPT; ++j) w[j] = __ldg(p + j * S);
+  };
+  // stage-1 operand: rows (2 lsp + pol) S + n2, columns (n1, re/im)
+  auto convert = [&]() {
+#pragma unroll
+    for (int g4 = 0; g4 < C::WPT / 4; ++g4) {
+      uint32_t h0[4], h1[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t x = __vmaxs4(w[4 * g4 + i], 0x81818181u) ^ 0x80808080u;
+        h0[i] = codes_to_h2(x, 0x4140);
+        h1[i] = codes_to_h2(x, 0x4342);
+      }
+      const int kc = n1_0 / 4 + g4;
+      const int m0 = (2 * lsp) * S + ln2, m1 = m0 + S;
+      *reinterpret_cast<uint4*>(sA1 + (m0 >> 3) * C::SBO + kc * C::LBO + (m0 & 7) * 16) =
+          make_uint4(h0[0], h0[1], h0[2], h0[3]);
+      *reinterpret_cast<uint4*>(sA1 + (m1 >> 3) * C::SBO + kc * C::LBO + (m1 & 7) * 16) =
+          make_uint4(h1[0], h1[1], h1[2], h1[3]);
+    }
+  };
+  // operands written and earlier tensor-memory loads complete -> MMAs
+  auto sync_for_mma = [&]() -> bool {
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    const int stop = __syncthreads_or(bad);
+    if (!stop && tid == 0) tc::fence_after_sync();
+    return stop != 0;
+  };
+  auto issue_s1 = [&]() {
+#pragma unroll
+    for (int ks = 0; ks < C::K / 16; ++ks)
+      tc::mma_f16(d1, tc::smem_desc(aA1 + ks * 2 * C::LBO, C::LBO, C::SBO),
+                  tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC, ks > 0 ? 1u : 0u);
+    tc::mma_commit(mb1);
+  };
+  // T hi x [F hi | F lo] + T lo x F hi (the lo x lo term is below 2^-22)
+  auto issue_s2 = [&]() {
+#pragma unroll
+    for (int ks = 0; ks < C::K / 16; ++ks)
+      tc::mma_f16(d2, tc::smem_desc(aHi + ks * 2 * C::LBO, C::LBO, C::SBO),
+                  tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC, ks > 0 ? 1u : 0u);
+#pragma unroll
+    for (int ks = 0; ks < C::K / 16; ++ks)
+      tc::mma_f16(d2, tc::smem_desc(aLo + ks * 2 * C::LBO, C::LBO, C::SBO),
+                  tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC_HI, 1u);
+    tc::mma_commit(mb2);
+  };
+  auto wait = [&](uint64_t* mb, unsigned& ph) {
+    if (!tc::mbar_wait_bounded(mb, ph, kTcWaitCycles)) bad = 1;
+    ph ^= 1;
+    tc::fence_after_sync();
+  };
+  // twiddle and hi/lo split: row seq S + k1, columns (n2 = r, re/im)
+  auto epi1 = [&]() {
+#pragma unroll
+    for (int q = 0; q < S / 8; ++q) {
+      float h[16], l[16];
+      tc::tmem_ld16x2(d1 + lane_off + 16 * q, d1 + lane_off + 2 * S + 16 * q, h, l);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int k1 = 8 * q + i;
+        const float2 y = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
+        const float2 tv = cmul(y, sTw[k1 * S + r]);
+        const __half2 hi = __floats2half2_rn(tv.x, tv.y);
+        const float2 hf = __half22float2(hi);
+        const __half2 lo = __floats2half2_rn(tv.x - hf.x, tv.y - hf.y);
+        const int mr = seq * S + k1;
+        const int off = (mr >> 3) * C::SBO + (r >> 2) * C::LBO + (mr & 7) * 16 + (r & 3) * 4;
+        *reinterpret_cast<__half2*>(sAhi + off) = hi;
+        *reinterpret_cast<__half2*>(sAlo + off) = lo;
+      }
+    }
+  };
+  // detection: lane seq S + k1 holds X[k1 + S k2] for all k2
+  auto epi2 = [&](float (&acc)[NACC]) {
+#pragma unroll
+    for (int q = 0; q < S / 8; ++q) {
+      float h[16], l[16];
+      tc::tmem_ld16x2(d2 + lane_off + 16 * q, d2 + lane_off + 2 * S + 16 * q, h, l);
+      float2 X[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) X[i] = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
+      if constexpr (POL == POL_TP) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          float s = acc[8 * q + i];
+          s = __fmaf_rn(X[i].x, X[i].x, s);
+          s = __fmaf_rn(X[i].y, X[i].y, s);
+          acc[8 * q + i] = s;
+        }
+      } else {
+        // the other polarisation of the same spectrum and k1 is lane tid ^ S
+        float2 Y[8];
+        if constexpr (S == 16) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            Y[i].x = __shfl_xor_sync(0xffffffffu, X[i].x, 16);
+            Y[i].y = __shfl_xor_sync(0xffffffffu, X[i].y, 16);
+          }
+        } else {
+          // exchange through the T lo area: its stage-2 MMAs have completed,
+          // and it is rewritten only after the barrier that ends this phase
+          float2* xb = reinterpret_cast<float2*>(sAlo) + (q & 1) * 128 * 8;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) xb[i * 128 + tid] = X[i];
+          __syncthreads();
+#pragma unroll
+          for (int i = 0; i < 8; ++i) Y[i] = xb[i * 128 + (tid ^ S)];
+        }
+        const bool p1 = (seq & 1) != 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const float2 x0 = p1 ? Y[i] : X[i], x1 = p1 ? X[i] : Y[i];
+          const float pw0 = __fmaf_rn(x0.x, x0.x, x0.y * x0.y);
+          const float pw1 = __fmaf_rn(x1.x, x1.x, x1.y * x1.y);
+          const int k2 = 8 * q + i;
+          if (!p1) {
+            acc[k2] += POL == POL_FULL ? pw0 : pw0 + pw1;
+            acc[S + k2] += __fmaf_rn(x0.x, x1.x, x0.y * x1.y);
+          } else {
+            acc[k2] += POL == POL_FULL ? pw1 : pw0 - pw1;
+            acc[S + k2] = __fmaf_rn(im_sign, __fmaf_rn(x0.y, x1.x, -(x0.x * x1.y)), acc[S + k2]);
+          }
+        }
+      }
+    }
+    if constexpr (POL != POL_TP && S > 16) __syncthreads();
+  };
+
   const int items = a.unit_count * a.chunks;
-  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+  bool stop = false;
+  for (int item = blockIdx.x; item < items && !stop; item += gridDim.x) {
     const int unit = a.unit0 + item / a.chunks, chunk = item % a.chunks;
     const int c = unit / a.units_per_chan, d = unit % a.units_per_chan;
     const int s_begin = chunk * a.spc;
@@ -126,149 +274,45 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
     const int ntiles = (s_end - s_begin) / SPT;
     const uint32_t* src = reinterpret_cast<const uint32_t*>(a.in) + (long long)c * a.chan_stride +
                           ((long long)d * a.M + s_begin + lsp) * N + (long long)n1_0 * S + ln2;
+    const long long tile_words = (long long)SPT * N;
 
     float acc[NACC];
 #pragma unroll
     for (int i = 0; i < NACC; ++i) acc[i] = 0.0f;
-    uint32_t w[C::WPT];
-#pragma unroll
-    for (int j = 0; j < C::WPT; ++j) w[j] = __ldg(src + j * S);
 
-    int stop = 0;
+    // prologue: tile 0 through stage 1 and into stage 2
+    load(src);
+    convert();
+    if (ntiles > 1) load(src + tile_words);
+    if ((stop = sync_for_mma())) break;
+    if (tid == 0) issue_s1();
+    wait(mb1, ph1);
+    epi1();
+    if ((stop = sync_for_mma())) break;
+    if (tid == 0) issue_s2();
+
     for (int t = 0; t < ntiles; ++t) {
-      // ---- stage-1 operand: rows (2 lsp + pol) S + n2, columns (n1, re/im)
-#pragma unroll
-      for (int g4 = 0; g4 < C::WPT / 4; ++g4) {
-        uint32_t h0[4], h1[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const uint32_t x = __vmaxs4(w[4 * g4 + i], 0x81818181u) ^ 0x80808080u;
-          h0[i] = codes_to_h2(x, 0x4140);
-          h1[i] = codes_to_h2(x, 0x4342);
-        }
-        const int kc = n1_0 / 4 + g4;
-        const int m0 = (2 * lsp) * S + ln2, m1 = m0 + S;
-        *reinterpret_cast<uint4*>(sAhi + (m0 >> 3) * C::SBO + kc * C::LBO + (m0 & 7) * 16) =
-            make_uint4(h0[0], h0[1], h0[2], h0[3]);
-        *reinterpret_cast<uint4*>(sAhi + (m1 >> 3) * C::SBO + kc * C::LBO + (m1 & 7) * 16) =
-            make_uint4(h1[0], h1[1], h1[2], h1[3]);
+      const bool more = t + 1 < ntiles;
+      if (more) {
+        // the stage-1 MMAs of tile t have completed: their operand is free
+        convert();
+        if (t + 2 < ntiles) load(src + (t + 2) * tile_words);
+        if ((stop = sync_for_mma())) break;
+        if (tid == 0) issue_s1();
       }
-      tc::fence_proxy_async_smem();
-      tc::fence_before_sync();
-      stop = __syncthreads_or(bad);
-      if (stop) break;
-      if (tid == 0) {
-        tc::fence_after_sync();
-#pragma unroll
-        for (int ks = 0; ks < C::K / 16; ++ks)
-          tc::mma_f16(tmem, tc::smem_desc(aHi + ks * 2 * C::LBO, C::LBO, C::SBO),
-                      tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC, ks > 0 ? 1u : 0u);
-        tc::mma_commit(mbar);
-      }
-      // the next tile's words are in flight during the MMAs
-      if (t + 1 < ntiles) {
-        const uint32_t* nsrc = src + (long long)(t + 1) * SPT * N;
-#pragma unroll
-        for (int j = 0; j < C::WPT; ++j) w[j] = __ldg(nsrc + j * S);
-      }
-      if (!tc::mbar_wait_bounded(mbar, phase, kTcWaitCycles)) bad = 1;
-      phase ^= 1;
-      tc::fence_after_sync();
-
-      // ---- twiddle and hi/lo split: row seq S + k1, columns (n2 = r, re/im)
-#pragma unroll
-      for (int q = 0; q < S / 8; ++q) {
-        float h[16], l[16];
-        tc::tmem_ld16x2(trow + 16 * q, trow + 2 * S + 16 * q, h, l);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int k1 = 8 * q + i;
-          const float2 y = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
-          const float2 tv = cmul(y, sTw[k1 * S + r]);
-          const __half2 hi = __floats2half2_rn(tv.x, tv.y);
-          const float2 hf = __half22float2(hi);
-          const __half2 lo = __floats2half2_rn(tv.x - hf.x, tv.y - hf.y);
-          const int mr = seq * S + k1;
-          const int off = (mr >> 3) * C::SBO + (r >> 2) * C::LBO + (mr & 7) * 16 + (r & 3) * 4;
-          *reinterpret_cast<__half2*>(sAhi + off) = hi;
-          *reinterpret_cast<__half2*>(sAlo + off) = lo;
-        }
-      }
-      tc::fence_proxy_async_smem();
-      tc::fence_before_sync();
-      stop = __syncthreads_or(bad);
-      if (stop) break;
-      if (tid == 0) {
-        tc::fence_after_sync();
-#pragma unroll
-        for (int ks = 0; ks < C::K / 16; ++ks)
-          tc::mma_f16(tmem, tc::smem_desc(aHi + ks * 2 * C::LBO, C::LBO, C::SBO),
-                      tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC, ks > 0 ? 1u : 0u);
-#pragma unroll
-        for (int ks = 0; ks < C::K / 16; ++ks)
-          tc::mma_f16(tmem, tc::smem_desc(aLo + ks * 2 * C::LBO, C::LBO, C::SBO),
-                      tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC, 1u);
-        tc::mma_commit(mbar);
-      }
-      if (!tc::mbar_wait_bounded(mbar, phase, kTcWaitCycles)) bad = 1;
-      phase ^= 1;
-      tc::fence_after_sync();
-
-      // ---- detection: lane seq S + k1 holds X[k1 + S k2] for all k2
-#pragma unroll
-      for (int q = 0; q < S / 8; ++q) {
-        float h[16], l[16];
-        tc::tmem_ld16x2(trow + 16 * q, trow + 2 * S + 16 * q, h, l);
-        float2 X[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) X[i] = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
-        if constexpr (POL == POL_TP) {
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            float s = acc[8 * q + i];
-            s = __fmaf_rn(X[i].x, X[i].x, s);
-            s = __fmaf_rn(X[i].y, X[i].y, s);
-            acc[8 * q + i] = s;
-          }
-        } else {
-          // the other polarisation of the same spectrum and k1 is lane tid ^ S
-          float2 Y[8];
-          if constexpr (S == 16) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              Y[i].x = __shfl_xor_sync(0xffffffffu, X[i].x, 16);
-              Y[i].y = __shfl_xor_sync(0xffffffffu, X[i].y, 16);
-            }
-          } else {
-            float2* xb = reinterpret_cast<float2*>(sAlo) + (q & 1) * 128 * 8;
-#pragma unroll
-            for (int i = 0; i < 8; ++i) xb[i * 128 + tid] = X[i];
-            __syncthreads();
-#pragma unroll
-            for (int i = 0; i < 8; ++i) Y[i] = xb[i * 128 + (tid ^ S)];
-          }
-          const bool p1 = (seq & 1) != 0;
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const float2 x0 = p1 ? Y[i] : X[i], x1 = p1 ? X[i] : Y[i];
-            const float pw0 = __fmaf_rn(x0.x, x0.x, x0.y * x0.y);
-            const float pw1 = __fmaf_rn(x1.x, x1.x, x1.y * x1.y);
-            const int k2 = 8 * q + i;
-            if (!p1) {
-              acc[k2] += POL == POL_FULL ? pw0 : pw0 + pw1;
-              acc[S + k2] += __fmaf_rn(x0.x, x1.x, x0.y * x1.y);
-            } else {
-              acc[k2] += POL == POL_FULL ? pw1 : pw0 - pw1;
-              acc[S + k2] = __fmaf_rn(im_sign, __fmaf_rn(x0.y, x1.x, -(x0.x * x1.y)), acc[S + k2]);
-            }
-          }
-        }
+      wait(mb2, ph2);
+      epi2(acc);
+      if (more) {
+        wait(mb1, ph1);
+        epi1();
+        if ((stop = sync_for_mma())) break;
+        if (tid == 0) issue_s2();
       }
     }
     if (stop) break;
 
     // ---- the unit's (chunk's) spectrum: fixed-order sum over the tile's sequences
-    if (__syncthreads_or(bad)) break;
+    if ((stop = __syncthreads_or(bad) != 0)) break;
     if constexpr (POL == POL_TP) {
 #pragma unroll
       for (int k2 = 0; k2 < S; ++k2) red[seq * N + r + S * k2] = acc[k2];
@@ -438,7 +482,7 @@ int tc_configure(TcLaunch& L, size_t* partial_floats, int pipe_groups) {
       cudaSuccess || tc_dispatch(L, nullptr, 2, &occ) != cudaSuccess || occ < 1)
     return -1;
   const int S = tc_side(L.logN), spt = 64 / S;
-  const int tmem_cols = std::max(32, 4 * S);
+  const int tmem_cols = 8 * S;
   occ = std::min(occ, 512 / tmem_cols);  // tensor-memory columns of the SM
   L.slots = occ * sms;
   L.smem = (L.logN == 8) ? TcCfg<16>::SMEM : (L.logN == 10) ? TcCfg<32>::SMEM : TcCfg<64>::SMEM;
