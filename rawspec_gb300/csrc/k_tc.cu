@@ -53,9 +53,10 @@ struct TcCfg {
   // stage-1 operand | T hi | T lo | DFT operand | twiddles | 2 mbarriers, tensor-memory slot
   static constexpr int SMEM = 3 * A_BYTES + TAB_BYTES + 32;
   static constexpr int TMEM_COLS = 2 * ND;    // stage-1 and stage-2 accumulators
-  static constexpr int MINB = 512 / TMEM_COLS;
-  static constexpr int WPT = S / 2;           // input words per thread per tile
-  static_assert(SPT * S == 64, "64 (spectrum, n2) pairs per tile, two threads each");
+  static constexpr int THREADS = 256;         // two warps per tensor-memory lane quarter
+  static constexpr int MINB = S == 16 ? 3 : 512 / TMEM_COLS;
+  static constexpr int WPT = S / 4;           // input words per thread per tile
+  static_assert(SPT * S == 64, "64 (spectrum, n2) pairs per tile, four threads each");
   static_assert(4 * SPT * (int)sizeof(float) * N <= 3 * A_BYTES, "reduction fits the operand area");
 };
 
@@ -79,12 +80,15 @@ __device__ __forceinline__ uint32_t codes_to_h2(uint32_t x, uint32_t sel) {
 // tile t is detected, and the stage-2 MMAs of tile t+1 while the codes of
 // tile t+2 are converted.  Each accumulator (stage 1, stage 2) has its own
 // tensor-memory columns and its own mbarrier; every shared-memory operand is
-// rewritten only after the MMAs reading it have completed.
+// rewritten only after the MMAs reading it have completed.  Warps w and w + 4
+// read the same tensor-memory lanes and split the accumulator columns
+// between them (8-column chunks q with q % 2 = w / 4).
 template <int S, int POL>
-__global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constant__ TcLaunch a) {
+__global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const __grid_constant__ TcLaunch a) {
   using C = TcCfg<S>;
   constexpr int N = C::N, NSEQ = C::NSEQ, SPT = C::SPT, NP = PolOut<POL>::NP;
-  constexpr int NACC = POL == POL_TP ? S : 2 * S;
+  constexpr int T = C::THREADS, NQ = S / 16;  // 8-column chunks per thread
+  constexpr int NACC = POL == POL_TP ? S / 2 : S;
   constexpr uint32_t IDESC = tc::idesc_f16_f32(128, C::ND);      // against [F hi | F lo]
   constexpr uint32_t IDESC_HI = tc::idesc_f16_f32(128, C::ND / 2);  // against F hi alone
   static_assert(POL == POL_TP || S <= 32, "cross-pol modes keep 2 S accumulators per thread");
@@ -103,7 +107,7 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
   {
     const uint4* src = reinterpret_cast<const uint4*>(a.tab);
     uint4* dst = reinterpret_cast<uint4*>(sB);
-    for (int i = tid; i < C::TAB_BYTES / 16; i += 128) dst[i] = __ldg(src + i);
+    for (int i = tid; i < C::TAB_BYTES / 16; i += T) dst[i] = __ldg(src + i);
   }
   if (tid == 0) {
     tc::mbar_init(mb1, 1);
@@ -118,17 +122,18 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
   const uint32_t d1 = tmem, d2 = tmem + C::ND;                       // accumulator columns
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;             // this warp's lanes
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;       // this warp's lanes
+  const int half = warp >> 2;                                        // its column chunks
   const uint32_t aA1 = tc::smem_u32(sA1), aHi = tc::smem_u32(sAhi), aLo = tc::smem_u32(sAlo);
   const uint32_t bF = tc::smem_u32(sB);
   unsigned ph1 = 0, ph2 = 0;
   int bad = 0;  // one of this thread's waits timed out
 
-  // input words: thread -> (spectrum of the tile, n2), half of the n1 range
-  const int pair = tid & 63, lsp = pair / S, ln2 = pair % S, n1_0 = (tid >> 6) * (S / 2);
+  // input words: thread -> (spectrum of the tile, n2), a quarter of the n1 range
+  const int pair = tid & 63, lsp = pair / S, ln2 = pair % S, n1_0 = (tid >> 6) * (S / 4);
   // tensor-memory lane of this thread: sequence seq, index r (n2 after stage
   // 1, k1 after stage 2)
-  const int seq = tid / S, r = tid % S;
+  const int lane_row = tid & 127, seq = lane_row / S, r = lane_row % S;
   const float im_sign = a.conj ? -1.0f : 1.0f;
 
   uint32_t w[C::WPT];
@@ -190,7 +195,8 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
   // twiddle and hi/lo split: row seq S + k1, columns (n2 = r, re/im)
   auto epi1 = [&]() {
 #pragma unroll
-    for (int q = 0; q < S / 8; ++q) {
+    for (int qq = 0; qq < NQ; ++qq) {
+      const int q = 2 * qq + half;
       float h[16], l[16];
       tc::tmem_ld16x2(d1 + lane_off + 16 * q, d1 + lane_off + 2 * S + 16 * q, h, l);
 #pragma unroll
@@ -211,7 +217,8 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
   // detection: lane seq S + k1 holds X[k1 + S k2] for all k2
   auto epi2 = [&](float (&acc)[NACC]) {
 #pragma unroll
-    for (int q = 0; q < S / 8; ++q) {
+    for (int qq = 0; qq < NQ; ++qq) {
+      const int q = 2 * qq + half;
       float h[16], l[16];
       tc::tmem_ld16x2(d2 + lane_off + 16 * q, d2 + lane_off + 2 * S + 16 * q, h, l);
       float2 X[8];
@@ -220,10 +227,10 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
       if constexpr (POL == POL_TP) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          float s = acc[8 * q + i];
+          float s = acc[8 * qq + i];
           s = __fmaf_rn(X[i].x, X[i].x, s);
           s = __fmaf_rn(X[i].y, X[i].y, s);
-          acc[8 * q + i] = s;
+          acc[8 * qq + i] = s;
         }
       } else {
         // the other polarisation of the same spectrum and k1 is lane tid ^ S
@@ -235,14 +242,14 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
             Y[i].y = __shfl_xor_sync(0xffffffffu, X[i].y, 16);
           }
         } else {
-          // exchange through the T lo area: its stage-2 MMAs have completed,
-          // and it is rewritten only after the barrier that ends this phase
-          float2* xb = reinterpret_cast<float2*>(sAlo) + (q & 1) * 128 * 8;
+          // exchange through the T areas: their stage-2 MMAs have completed,
+          // and they are rewritten only after the barrier that ends this phase
+          float2* xb = reinterpret_cast<float2*>(sAhi) + (2 * half + (qq & 1)) * 128 * 8;
 #pragma unroll
-          for (int i = 0; i < 8; ++i) xb[i * 128 + tid] = X[i];
+          for (int i = 0; i < 8; ++i) xb[i * 128 + lane_row] = X[i];
           __syncthreads();
 #pragma unroll
-          for (int i = 0; i < 8; ++i) Y[i] = xb[i * 128 + (tid ^ S)];
+          for (int i = 0; i < 8; ++i) Y[i] = xb[i * 128 + (lane_row ^ S)];
         }
         const bool p1 = (seq & 1) != 0;
 #pragma unroll
@@ -250,13 +257,13 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
           const float2 x0 = p1 ? Y[i] : X[i], x1 = p1 ? X[i] : Y[i];
           const float pw0 = __fmaf_rn(x0.x, x0.x, x0.y * x0.y);
           const float pw1 = __fmaf_rn(x1.x, x1.x, x1.y * x1.y);
-          const int k2 = 8 * q + i;
+          const int j = 8 * qq + i;
           if (!p1) {
-            acc[k2] += POL == POL_FULL ? pw0 : pw0 + pw1;
-            acc[S + k2] += __fmaf_rn(x0.x, x1.x, x0.y * x1.y);
+            acc[j] += POL == POL_FULL ? pw0 : pw0 + pw1;
+            acc[S / 2 + j] += __fmaf_rn(x0.x, x1.x, x0.y * x1.y);
           } else {
-            acc[k2] += POL == POL_FULL ? pw1 : pw0 - pw1;
-            acc[S + k2] = __fmaf_rn(im_sign, __fmaf_rn(x0.y, x1.x, -(x0.x * x1.y)), acc[S + k2]);
+            acc[j] += POL == POL_FULL ? pw1 : pw0 - pw1;
+            acc[S / 2 + j] = __fmaf_rn(im_sign, __fmaf_rn(x0.y, x1.x, -(x0.x * x1.y)), acc[S / 2 + j]);
           }
         }
       }
@@ -313,19 +320,21 @@ __global__ void __launch_bounds__(128, TcCfg<S>::MINB) k_tc(const __grid_constan
 
     // ---- the unit's (chunk's) spectrum: fixed-order sum over the tile's sequences
     if ((stop = __syncthreads_or(bad) != 0)) break;
+    // bin k1 + S k2 of this thread: k2 = 8 (2 qq + half) + i for its acc[8 qq + i]
     if constexpr (POL == POL_TP) {
 #pragma unroll
-      for (int k2 = 0; k2 < S; ++k2) red[seq * N + r + S * k2] = acc[k2];
+      for (int j = 0; j < S / 2; ++j) red[seq * N + r + S * (8 * (2 * (j / 8) + half) + j % 8)] = acc[j];
     } else {
       const int sp = seq >> 1, pl = seq & 1;
 #pragma unroll
-      for (int k2 = 0; k2 < S; ++k2) {
-        red[(pl * SPT + sp) * N + r + S * k2] = acc[k2];
-        red[((pl + 2) * SPT + sp) * N + r + S * k2] = acc[S + k2];
+      for (int j = 0; j < S / 2; ++j) {
+        const int k2 = 8 * (2 * (j / 8) + half) + j % 8;
+        red[(pl * SPT + sp) * N + r + S * k2] = acc[j];
+        red[((pl + 2) * SPT + sp) * N + r + S * k2] = acc[S / 2 + j];
       }
     }
     __syncthreads();
-    for (int o = tid; o < NP * N; o += 128) {
+    for (int o = tid; o < NP * N; o += T) {
       const int pl = o / N, k = o - pl * N;
       float s = 0.0f;
       if constexpr (POL == POL_TP) {
@@ -393,12 +402,12 @@ cudaError_t tc_launch_t(const TcLaunch& L, cudaStream_t s, int op, int* occ) {
   if (op != 0) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess || op == 1) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k, 128, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k, TcCfg<S>::THREADS, smem);
   }
   const int items = L.unit_count * L.chunks;
   const int grid = std::min(items, std::max(L.slots, 1));
   if (grid < 1) return cudaSuccess;
-  k<<<grid, 128, smem, s>>>(L);
+  k<<<grid, TcCfg<S>::THREADS, smem, s>>>(L);
   return cudaGetLastError();
 }
 
