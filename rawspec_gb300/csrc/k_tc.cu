@@ -29,6 +29,8 @@
 // FFT-shifted store (or per-chunk partial sums, finished by k_finalize).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cuda_fp16.h>
 
 #include "detect.cuh"
@@ -401,8 +403,24 @@ cudaError_t tc_launch_t(const TcLaunch& L, cudaStream_t s, int op, int* occ) {
   constexpr int smem = TcCfg<S>::SMEM;
   if (op != 0) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    // the whole unified L1/shared array as shared memory, so that the
+    // occupancy query (and the launch) count on the largest carveout
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess || op == 1) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k, TcCfg<S>::THREADS, smem);
+    // resident CTAs per SM from the kernel's registers and shared memory
+    // (computed here: the occupancy query reports one CTA per SM for this
+    // kernel, where the hardware places two)
+    cudaFuncAttributes fa;
+    int dev = 0, regs_sm = 0, smem_sm = 0, smem_rsv = 0;
+    if ((e = cudaFuncGetAttributes(&fa, k)) != cudaSuccess || (e = cudaGetDevice(&dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+      return e;
+    const int regs_cta = ((fa.numRegs + 7) / 8 * 8) * TcCfg<S>::THREADS;
+    *occ = std::min(regs_sm / std::max(regs_cta, 1), smem_sm / (smem + smem_rsv));
+    return cudaSuccess;
   }
   const int items = L.unit_count * L.chunks;
   const int grid = std::min(items, std::max(L.slots, 1));
@@ -505,6 +523,10 @@ int tc_configure(TcLaunch& L, size_t* partial_floats, int pipe_groups) {
   *partial_floats = cmax > 1 ? (size_t)L.n_units * cmax * np * ((size_t)1 << L.logN) : 0;
   L.unit0 = 0;
   L.unit_count = L.n_units;
+  if (getenv("RAWSPEC_GB300_VERBOSE"))
+    fprintf(stderr, "k_tc: N %d, pol %d, units %d x %d spectra, %d resident CTAs (%d per SM), %d chunks of %d "
+                    "spectra (%d of %d per channel group)\n", 1 << L.logN, L.pol, L.n_units, L.M, L.slots, occ,
+            L.chunks, L.spc, L.chunks_pipe, L.spc_pipe);
   return 0;
 }
 
