@@ -414,7 +414,7 @@ def run_native(args, rank, world, local_rank):
     e2e = whole_job_gbs(world, step_bytes, args.steps, r["e2e_s"])
     # dominant kernel class of the headline run
     prof = r["prof"]
-    kernel_classes = ["small", "finalize", "large_a", "large_b", "ics", "expand4", "large_fused"]
+    kernel_classes = ["small", "finalize", "large_a", "large_b", "ics", "expand4", "large_fused", "tc"]
     t_large = prof["large_a"][0] + prof["large_b"][0]
     dom = max(kernel_classes, key=lambda k: t_large if k in ("large_a", "large_b") else prof[k][0])
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}

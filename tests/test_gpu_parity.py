@@ -56,7 +56,10 @@ def oracle_for(c, blocks, weights=None, inverse=None):
 
 @pytest.mark.parametrize("logn", list(range(0, 13)))
 @pytest.mark.parametrize("npol", [1, 4, -4])
-def test_small_lengths_all_modes(cuda_device, logn, npol):
+def test_small_lengths_all_modes(cuda_device, monkeypatch, logn, npol):
+    # the CUDA-core kernel k_small at every length (the tensor-core kernel,
+    # the default at 1024 points, has its own tests)
+    monkeypatch.setenv("RAWSPEC_GB300_TENSOR_DFT", "0")
     nt = 1 << logn
     Ntpb = max(4096, nt)
     # Na chosen so that some integrations stay within the buffer (Nd > 1),

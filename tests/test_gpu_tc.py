@@ -4,8 +4,10 @@ FP32 accumulation in tensor memory) against the FP64 oracle.
 First the MMA building block alone: a host-built shared-memory image of two
 K-major FP16 operands goes through the library's descriptors and MMA
 wrappers (tests/probe/umma_probe.cu) and must give the exact integer matrix
-product.  Then whole products with RAWSPEC_GB300_TENSOR_DFT=1, every mode,
-direction, integration spanning buffers and the pipelined combined call."""
+product.  Then whole products with RAWSPEC_GB300_TENSOR_DFT=1 (the kernel
+for every length it supports: 256, 1024, 4096), every mode, direction,
+integration spanning buffers and the pipelined combined call.  The errors
+against the oracle are printed (pytest -s) as well as checked."""
 import ctypes as C
 import subprocess
 from pathlib import Path
@@ -108,6 +110,7 @@ def test_tensor_dft_matches_oracle(cuda_device, monkeypatch, logn, npol, na, con
     ref = oracle_for(c, blocks)
     assert got[0].shape == ref[0].shape
     err = normalized_error(got[0], ref[0], npol, 3, nt)
+    print(f"k_tc N={nt} Npolout={npol} Na={na} conj={conj} fft_dir={fft_dir}: normalized error {err:.2e}")
     assert err < REL_TOL, (nt, npol, err)
 
 
@@ -123,7 +126,9 @@ def test_tensor_dft_integration_across_buffers(cuda_device, monkeypatch, npol):
     assert n_tc > 0
     ref = oracle_for(c, blocks)
     assert got[0].shape == ref[0].shape
-    assert normalized_error(got[0], ref[0], npol, 2, nt) < REL_TOL
+    err = normalized_error(got[0], ref[0], npol, 2, nt)
+    print(f"k_tc N={nt} Npolout={npol} Na=96 over six buffers: normalized error {err:.2e}")
+    assert err < REL_TOL
 
 
 @pytest.mark.parametrize("nbits", [8, 4])
