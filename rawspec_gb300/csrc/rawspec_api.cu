@@ -179,14 +179,16 @@ bool is_pow2(unsigned x) { return x && !(x & (x - 1)); }
 int ilog2u(unsigned x) { int l = 0; while ((1u << l) < x) ++l; return l; }
 
 // Which products of 8-bit input run their DFT on the tensor cores (k_tc)
-// rather than in k_small: by default those of N = 1024, where k_tc is at
-// least as fast; RAWSPEC_GB300_TENSOR_DFT=1 at initialisation selects it for
-// every length it supports (256, 1024, 4096), =0 for none.
-bool tensor_dft_wanted(int logN) {
+// rather than in k_small: by default the total-power products of N = 1024,
+// where k_tc is at least as fast and overlaps better with the other
+// products' CUDA-core kernels; RAWSPEC_GB300_TENSOR_DFT=1 at initialisation
+// selects it for every case it supports (N = 256, 1024, 4096, all modes up to
+// 1024), =0 for none.
+bool tensor_dft_wanted(int logN, int pol) {
   const char* v = getenv("RAWSPEC_GB300_TENSOR_DFT");
   if (v && v[0] == '0') return false;
   if (v && v[0] == '1') return true;
-  return logN == 10;
+  return logN == 10 && pol == POL_TP;
 }
 
 int validate_impl(rawspec_context* ctx, bool* expanded) {
@@ -689,7 +691,7 @@ int rawspec_initialize(rawspec_context* ctx) {
     }
 
     P.large = P.logN > 12;
-    P.tc = !P.large && tensor_dft_wanted(P.logN) && tc_supported(P.logN, g->fmt, (int)ctx->Np, pol, M);
+    P.tc = !P.large && tensor_dft_wanted(P.logN, pol) && tc_supported(P.logN, g->fmt, (int)ctx->Np, pol, M);
     if (P.tc) {
       TcLaunch& L = P.tl;
       L.logN = P.logN;
