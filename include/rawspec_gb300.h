@@ -67,6 +67,12 @@ unsigned long long rawspec_gb300_kernel_launches(rawspec_context *ctx);
 /* Bytes of device memory held by the context. */
 size_t rawspec_gb300_device_bytes(rawspec_context *ctx);
 
+/* Device memory rawspec_initialize() would allocate for this context (the
+ * same validation and kernel configuration, nothing allocated; the context
+ * itself is not modified).  Needs the CUDA device gpu_index.  0 on success,
+ * 1 if the context is invalid. */
+int rawspec_gb300_device_bytes_estimate(const rawspec_context *ctx, size_t *bytes);
+
 /* Allocation-free computation of one output product for one device-resident
  * input buffer.  No counterpart in the reference library.
  *

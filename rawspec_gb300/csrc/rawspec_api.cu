@@ -544,6 +544,91 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
 
 }  // namespace
 
+// Device bytes rawspec_initialize() allocates for a validated context: the
+// same sizes, from the same configuration functions, without allocating.
+int plan_device_bytes(const rawspec_context* ctx, bool expanded, int sm_count, size_t* total) {
+  size_t t = 0;
+  const int fmt = ctx->Nbps == 16 ? FMT_I16 : FMT_I8;
+  const size_t blk_bytes = (size_t)ctx->Ntpb * ctx->Np * ctx->Nc * 2 * (ctx->Nbps / 8);
+  const size_t in_bytes = blk_bytes * ctx->Nb;
+  t += in_bytes;
+  if (expanded) t += in_bytes / 2;
+  if (ctx->incoherently_sum) t += ctx->Nant * sizeof(float);
+  const int target_ctas = sm_count * 4;
+  const int groups = std::min<int>(kMaxCopyGroups, (int)ctx->Nc);
+  auto al = [](size_t n) { return (n + 31) & ~size_t(31); };
+  for (unsigned i = 0; i < ctx->No; i++) {
+    const int N = (int)ctx->Nts[i], logN = ilog2u(ctx->Nts[i]), np = abs(ctx->Npolout[i]);
+    unsigned Nss, Nis, Nd;
+    derived(ctx, (int)i, &Nss, &Nis, &Nd);
+    const int pol = np == 1 ? POL_TP : ctx->Npolout[i];
+    const int M = (int)(Nis > 1 ? Nss : ctx->Nas[i]);
+    const int upc = (int)(Nis > 1 ? 1 : Nss / ctx->Nas[i]);
+    t += ctx->h_pwrbuf_size[i];
+    if (ctx->incoherently_sum) t += ctx->h_pwrbuf_size[i] / ctx->Nant;
+    const bool large = logN > 12;
+    if (!large && tensor_dft_wanted(logN, pol) && tc_supported(logN, fmt, (int)ctx->Np, pol, M)) {
+      TcLaunch L;
+      L.logN = logN;
+      L.pol = pol;
+      L.Nc = (int)ctx->Nc;
+      L.M = M;
+      L.units_per_chan = upc;
+      L.n_units = (int)ctx->Nc * upc;
+      size_t pf = 0;
+      if (tc_configure(L, &pf, groups)) return 1;
+      t += pf * sizeof(float) + ((tc_table_bytes(logN) + 15) & ~size_t(15)) + sizeof(int);
+    } else if (!large) {
+      SmallLaunch L;
+      L.logN = logN;
+      L.fmt = fmt;
+      L.nv = (int)ctx->Np;
+      L.pol = pol;
+      L.Nc = (int)ctx->Nc;
+      L.M = M;
+      L.units_per_chan = upc;
+      L.n_units = (int)ctx->Nc * upc;
+      L.chan_stride = (long long)ctx->Nb * ctx->Ntpb;
+      size_t pf = 0;
+      if (small_configure(L, target_ctas, &pf, groups)) return 1;
+      t += pf * sizeof(float) + (size_t)std::max(stockham_table_size(N, small_radix(logN, pol)), 1) * sizeof(float2);
+    } else {
+      LargeLaunch L;
+      L.logN = logN;
+      L.fmt = fmt;
+      L.nv = (int)ctx->Np;
+      L.pol = pol;
+      L.Nc = (int)ctx->Nc;
+      L.Nss = (int)Nss;
+      L.M = M;
+      L.units_per_chan = upc;
+      L.n_units = (int)ctx->Nc * upc;
+      L.chan_stride = (long long)ctx->Nb * ctx->Ntpb;
+      size_t sf = 0, pf = 0;
+      if (large_configure(L, target_ctas, &sf, &pf)) return 1;
+      const bool fused = large_fused_supported(L);
+      if (fused) {
+        L.S = (int)ctx->Nc * (int)Nss;
+        if (large_fused_plan(L) != cudaSuccess) return 1;
+        sf = (size_t)std::min(L.ring, L.S) * L.nv * ((size_t)1 << L.logN);
+        pf = 0;
+        t += (size_t)large_fused_ctl_ints(L) * sizeof(int);
+      }
+      t += sf * sizeof(float2) + pf * sizeof(float);
+      const int n1 = 1 << L.logN1, n2 = 1 << L.logN2;
+      const int RA = fused ? large_fused_col_radix() : large_pass_a_radix();
+      const int RB = fused ? large_fused_row_radix(pol) : large_pass_b_radix(pol);
+      const size_t ta = (size_t)stockham_table_size(n2, RA), tb = (size_t)stockham_table_size(n1, RB);
+      const size_t nlo = (size_t)1 << L.h, nhi = (size_t)1 << (L.logN - L.h), nm = (size_t)RA * n1;
+      const size_t nj = fused ? (size_t)large_fused_twj_entries(L) : 0;
+      const size_t o_j = al(ta) + al(tb) + al(nlo) + al(nhi) + al(nm);
+      t += (o_j + nj) * sizeof(float2);
+    }
+  }
+  *total = t;
+  return 0;
+}
+
 // ============================================================================
 // Public C interface (the only symbols the library exports).
 // ============================================================================
@@ -1106,6 +1191,20 @@ unsigned long long rawspec_gb300_kernel_launches(rawspec_context* ctx) {
 size_t rawspec_gb300_device_bytes(rawspec_context* ctx) {
   GpuCtx* g = G(ctx);
   return g ? g->device_bytes : 0;
+}
+
+int rawspec_gb300_device_bytes_estimate(const rawspec_context* ctx, size_t* bytes) {
+  if (!ctx || !bytes) return 1;
+  rawspec_context c = *ctx;  // validation normalises fields of its own copy
+  bool expanded = false;
+  if (validate_impl(&c, &expanded)) return 1;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (dev != c.gpu_index && cudaSetDevice(c.gpu_index) != cudaSuccess) return 1;
+  const bool ok = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.gpu_index) == cudaSuccess &&
+                  plan_device_bytes(&c, expanded, sms, bytes) == 0;
+  if (dev != c.gpu_index) cudaSetDevice(dev);
+  return ok ? 0 : 1;
 }
 
 }  // extern "C"
