@@ -275,6 +275,85 @@ def ingest_leg(nbuf: int = 8) -> dict:
                       "files written by the dump callback"}
 
 
+def serving_leg(njobs: int = 256, rate: float = 40.0, budget: float = 120e9) -> dict:
+    """The serving mix (rawspec_gb300.mix: jobs of 2-16 blocks, Nchan 8/32/64,
+    4/8-bit, 1-3 products of Nfft 8 ... 2^20) through the job server under a
+    120 GB device-memory budget: once with the Poisson arrivals (mean 40 jobs
+    per second) and once with every job submitted at the start (capacity);
+    beside them a serial plain-path replay of the same jobs (a context per job,
+    one after another).  RAW bytes over wall clock; latencies from the push of
+    a buffer (its data in pinned memory) to its processing complete, and to the
+    POST_DUMP of the dumps it ends."""
+    import numpy as np
+
+    from rawspec_gb300 import api, mix, serve
+    jobs = mix.serving_jobs(njobs, rate)
+    bufs = [mix.block_bytes(j) * j["Nb"] for j in jobs]
+    pool = np.random.default_rng(9).integers(-128, 128, size=max(bufs), dtype=np.int16).astype(np.uint8)
+    total = sum(mix.block_bytes(j) * j["blocks"] for j in jobs)
+
+    def served(on_schedule: bool) -> dict:
+        srv = serve.Server(int(budget), max_active=16, max_queued=2, collect=False)
+        try:
+            def feed(k, jid):
+                for _ in range(jobs[k]["blocks"] // jobs[k]["Nb"]):
+                    srv.push(jid, pool[:bufs[k]])
+                srv.close_job(jid)
+            threads = []
+            t0 = time.perf_counter()
+            for k, j in enumerate(jobs):
+                if on_schedule:
+                    dt = t0 + j["arrival"] - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                jid = srv.submit(j["Nc"], 2, j["ntpb"], j["nbits"], j["products"], Nb=j["Nb"])
+                th = threading.Thread(target=feed, args=(k, jid))
+                th.start()
+                threads.append((jid, th))
+            for jid, th in threads:
+                th.join()
+            states = [srv.wait_job(jid, 600.0) for jid, _ in threads]
+            secs = time.perf_counter() - t0
+            st = srv.stats()
+        finally:
+            srv.close()
+        if any(x != serve.JOB_DONE for x in states):
+            raise RuntimeError("serving mix: a job failed")
+        return {"value": total / secs / 1e9, "unit": "GB/s", "seconds": secs, "jobs_per_s": njobs / secs,
+                "buffers": int(st.buffers), "dumps": int(st.dumps), "peak_active_jobs": int(st.peak_active),
+                "peak_device_bytes": int(st.peak_used),
+                "buffer_ms_p50": st.buffer_p50_ms, "buffer_ms_p99": st.buffer_p99_ms,
+                "dump_ms_p50": st.dump_p50_ms, "dump_ms_p99": st.dump_p99_ms}
+
+    arrivals = served(True)
+    burst = served(False)
+    # serial plain path: one context per job, the CLI's per-buffer calls
+    lat = []
+    t0 = time.perf_counter()
+    for k, j in enumerate(jobs):
+        spec = api.Spectrometer(j["Nc"], 2, j["ntpb"], j["nbits"], j["products"], Nb=j["Nb"], collect=False)
+        try:
+            blocks = pool[:bufs[k]].reshape(j["Nb"], -1)
+            for _ in range(j["blocks"] // j["Nb"]):
+                spec.load_blocks(blocks)
+                ts = time.perf_counter()
+                spec.copy_and_start()
+                if spec.wait() != 0:
+                    raise RuntimeError("serial replay failed")
+                lat.append(1e3 * (time.perf_counter() - ts))
+        finally:
+            spec.close()
+    serial_s = time.perf_counter() - t0
+    return {"workload": f"{njobs} jobs, Poisson arrivals at {rate:g} jobs/s, 2-16 blocks of Ntpb 262144, "
+                        "Nchan 8/32/64, 4/8-bit, 1-3 products of Nfft 8/1024/65536/1048576, Nint 16-3072, "
+                        f"Npolout 1/4/-4; {budget / 1e9:g} GB device-memory budget",
+            "raw_bytes": total, "arrivals": arrivals, "all_at_start": burst,
+            "serial_plain": {"value": total / serial_s / 1e9, "unit": "GB/s", "seconds": serial_s,
+                             "buffer_ms_p50": float(np.percentile(lat, 50)),
+                             "buffer_ms_p99": float(np.percentile(lat, 99))},
+            "speedup_vs_serial": serial_s / burst["seconds"]}
+
+
 def run_reference(args, rank, world):
     """CPU restatement of the chain (kind "port") with all host threads."""
     if rank != 0:
@@ -482,6 +561,8 @@ def run_native(args, rank, world, local_rank):
         line["cpu_baseline"] = cpu_baseline_leg()
     if rank == 0 and world == 1 and not args.no_ingest:
         line["ingest"] = ingest_leg()
+    if rank == 0 and world == 1 and not args.no_serve:
+        line["serving"] = serving_leg()
     if rank == 0:
         print(json.dumps(line), flush=True)
     group.close()
@@ -496,6 +577,7 @@ def main():
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-ingest", action="store_true", help="skip the RAW-file ingest leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-mix leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local_rank = rank_info()

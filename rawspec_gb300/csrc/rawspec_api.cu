@@ -107,7 +107,8 @@ struct GpuCtx {
   Product prod[MAX_OUTPUTS];
   unsigned inbuf_count = 0;
   bool caller_managed = false;
-  unsigned registered = 0;  // caller blocks page-locked so far
+  unsigned registered = 0;  // caller blocks examined (and page-locked unless they already were) so far
+  std::vector<char> locked_here;  // per caller block: page-locked by this library (unlocked at cleanup)
   DumpCb cb[MAX_OUTPUTS];
   size_t device_bytes = 0;
   unsigned long long launches = 0;
@@ -723,8 +724,17 @@ int rawspec_initialize(rawspec_context* ctx) {
       CK(cudaHostAlloc((void**)&ctx->h_blkbufs[i], blk_bytes, cudaHostAllocDefault));
   } else {
     g->caller_managed = true;
+    g->locked_here.assign(ctx->Nb_host, 0);
     for (unsigned i = 0; i < ctx->Nb_host; i++) {
-      CK(cudaHostRegister(ctx->h_blkbufs[i], blk_bytes, cudaHostRegisterDefault));
+      // blocks the caller already page-locked (cudaHostAlloc) are used as they are
+      cudaPointerAttributes pa;
+      const bool pinned = cudaPointerGetAttributes(&pa, ctx->h_blkbufs[i]) == cudaSuccess &&
+                          pa.type == cudaMemoryTypeHost;
+      cudaGetLastError();
+      if (!pinned) {
+        CK(cudaHostRegister(ctx->h_blkbufs[i], blk_bytes, cudaHostRegisterDefault));
+        g->locked_here[i] = 1;
+      }
       g->registered = i + 1;
     }
   }
@@ -925,7 +935,8 @@ void rawspec_cleanup(rawspec_context* ctx) {
   if (!g) return;
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->caller_managed) {
-    for (unsigned i = 0; i < g->registered; i++) cudaHostUnregister(ctx->h_blkbufs[i]);
+    for (unsigned i = 0; i < g->registered; i++)
+      if (g->locked_here[i]) cudaHostUnregister(ctx->h_blkbufs[i]);
   } else if (ctx->h_blkbufs) {
     for (unsigned i = 0; i < ctx->Nb_host; i++)
       if (ctx->h_blkbufs[i]) cudaFreeHost(ctx->h_blkbufs[i]);

@@ -14,9 +14,11 @@
 // others run starts as soon as it fits.
 //
 // Pushed buffers are copied by the pushing thread into the job's pool of
-// pinned host slots; the loop points the context's host blocks at the slot
-// for the call (the library's own blocks are put back before the context is
-// freed), so the request loop copies no data itself.
+// pinned host slots, which are the context's host blocks (caller-managed):
+// the loop points the context's block pointers at the slot of the buffer for
+// the call, so the request loop copies no data itself.  Slots return to a
+// server-wide cache of pinned buffers when their job ends, so that jobs do
+// not pay for page-locking memory.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -58,10 +60,10 @@ struct Job {
   void* user = nullptr;
   int state = RAWSPEC_GB300_JOB_PENDING;
   bool closed = false;
-  std::vector<char*> pool;      // pinned slots
+  std::vector<std::pair<char*, size_t>> pool;  // pinned slots and their capacities
   std::vector<char*> free_slots;
   std::deque<Slot> queue;
-  std::vector<char*> own_blocks;  // the library's host blocks, restored before cleanup
+  std::vector<char*> blocks;     // the context's host block pointers (caller-managed)
   bool inflight = false;
   Slot cur;                      // the buffer in flight
   std::atomic<double> t_inflight{0.0};
@@ -100,6 +102,9 @@ void job_dump_cb(rawspec_context* ctx, int product, int type) {
 
 struct rawspec_gb300_server {
   int gpu = 0;
+  std::mutex cache_mu;
+  std::multimap<size_t, char*> cache;  // pinned buffers of finished jobs, by capacity
+  size_t cache_bytes = 0;
   size_t budget = 0;
   int max_active = 1, max_queued = 2;
   std::mutex mu;
@@ -116,8 +121,40 @@ struct rawspec_gb300_server {
 
 namespace {
 
-void free_pool(Job* j) {
-  for (char* p : j->pool) cudaFreeHost(p);
+constexpr size_t kCacheCap = size_t(8) << 30;  // pinned bytes kept for later jobs
+
+char* take_pinned(rawspec_gb300_server* s, size_t bytes, size_t* cap) {
+  {
+    std::lock_guard<std::mutex> g(s->cache_mu);
+    auto it = s->cache.lower_bound(bytes);
+    if (it != s->cache.end() && it->first <= 2 * bytes) {
+      char* p = it->second;
+      *cap = it->first;
+      s->cache_bytes -= it->first;
+      s->cache.erase(it);
+      return p;
+    }
+  }
+  char* p = nullptr;
+  if (cudaHostAlloc((void**)&p, bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  *cap = bytes;
+  return p;
+}
+
+void give_pinned(rawspec_gb300_server* s, char* p, size_t cap) {
+  {
+    std::lock_guard<std::mutex> g(s->cache_mu);
+    if (s->cache_bytes + cap <= kCacheCap) {
+      s->cache.emplace(cap, p);
+      s->cache_bytes += cap;
+      return;
+    }
+  }
+  cudaFreeHost(p);
+}
+
+void free_pool(rawspec_gb300_server* s, Job* j) {
+  for (auto& pc : j->pool) give_pinned(s, pc.first, pc.second);
   j->pool.clear();
   j->free_slots.clear();
 }
@@ -147,11 +184,10 @@ void request_loop(rawspec_gb300_server* s) {
       const int rc = rawspec_initialize(&j->ctx);
       lk.lock();
       if (rc) {
-        free_pool(j);
+        free_pool(s, j);
         retire(s, j, RAWSPEC_GB300_JOB_FAILED);
         continue;
       }
-      j->own_blocks.assign(j->ctx.h_blkbufs, j->ctx.h_blkbufs + j->ctx.Nb_host);
       const size_t actual = rawspec_gb300_device_bytes(&j->ctx);
       if (actual > j->est) {  // never expected: the estimate repeats the allocation plan
         s->used += actual - j->est;
@@ -184,11 +220,10 @@ void request_loop(rawspec_gb300_server* s) {
         j->cur = j->queue.front();
         j->queue.pop_front();
         lk.unlock();
-        for (unsigned b = 0; b < j->ctx.Nb; b++) j->ctx.h_blkbufs[b] = j->cur.data + b * j->blk_bytes;
+        for (unsigned b = 0; b < j->ctx.Nb; b++) j->blocks[b] = j->cur.data + b * j->blk_bytes;
         j->t_inflight.store(j->cur.t_push);
         const int rc =
             rawspec_copy_blocks_to_gpu_and_start_processing(&j->ctx, j->ctx.Nb, j->expand4, j->fft_dir);
-        for (unsigned b = 0; b < j->ctx.Nb; b++) j->ctx.h_blkbufs[b] = j->own_blocks[b];
         lk.lock();
         j->free_slots.push_back(j->cur.data);  // the host blocks may be reused once the call returns
         s->cv_state.notify_all();
@@ -198,7 +233,7 @@ void request_loop(rawspec_gb300_server* s) {
           rawspec_wait_for_completion(&j->ctx);
           rawspec_cleanup(&j->ctx);
           lk.lock();
-          free_pool(j);
+          free_pool(s, j);
           retire(s, j, RAWSPEC_GB300_JOB_FAILED);
           continue;
         }
@@ -209,7 +244,7 @@ void request_loop(rawspec_gb300_server* s) {
         const int rc = rawspec_wait_for_completion(&j->ctx);
         rawspec_cleanup(&j->ctx);
         lk.lock();
-        free_pool(j);
+        free_pool(s, j);
         retire(s, j, rc ? RAWSPEC_GB300_JOB_FAILED : RAWSPEC_GB300_JOB_DONE);
         progress = true;
       }
@@ -266,8 +301,6 @@ int rawspec_gb300_server_submit(rawspec_gb300_server* s, const rawspec_context* 
     c.Nas[i] = job->Nas[i];
   }
   c.Nb = job->Nb;
-  c.Nb_host = 0;
-  c.h_blkbufs = nullptr;
   c.gpu_index = s->gpu;
   c.input_conjugated = job->input_conjugated;
   c.incoherently_sum = job->incoherently_sum;
@@ -291,18 +324,25 @@ int rawspec_gb300_server_submit(rawspec_gb300_server* s, const rawspec_context* 
   c.dump_callback = job_dump_cb;
   c.user_data = j.get();
   for (int k = 0; k < s->max_queued; k++) {
-    char* p = nullptr;
-    if (cudaHostAlloc((void**)&p, j->blk_bytes * v.Nb, cudaHostAllocDefault) != cudaSuccess) {
-      free_pool(j.get());
+    size_t cap = 0;
+    char* p = take_pinned(s, j->blk_bytes * v.Nb, &cap);
+    if (!p) {
+      free_pool(s, j.get());
       return -1;
     }
-    j->pool.push_back(p);
+    j->pool.emplace_back(p, cap);
     j->free_slots.push_back(p);
   }
+  // the context's host blocks are the slots (already page-locked, so the
+  // library uses them as they are); the loop points them at each buffer
+  j->blocks.resize(v.Nb);
+  for (unsigned b = 0; b < v.Nb; b++) j->blocks[b] = j->pool[0].first + b * j->blk_bytes;
+  c.h_blkbufs = j->blocks.data();
+  c.Nb_host = v.Nb;
   j->t_submit = now_s();
   std::lock_guard<std::mutex> g(s->mu);
   if (s->stop) {
-    free_pool(j.get());
+    free_pool(s, j.get());
     return -1;
   }
   const int id = s->next_id++;
@@ -418,7 +458,8 @@ void rawspec_gb300_server_destroy(rawspec_gb300_server* s) {
     s->cv_loop.notify_all();
   }
   s->loop.join();
-  for (auto& kv : s->jobs) free_pool(kv.second.get());
+  for (auto& kv : s->jobs) free_pool(s, kv.second.get());
+  for (auto& kv : s->cache) cudaFreeHost(kv.second);
   delete s;
 }
 
