@@ -18,6 +18,8 @@
 //  * PRE_DUMP is queued before any write to h_pwrbuf/h_icsbuf of a dump and
 //    POST_DUMP after both, on the processing stream (cudaLaunchHostFunc).
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -366,6 +368,74 @@ void CUDART_CB post_dump_fn(void* data) {
   if (d->ctx->dump_callback) d->ctx->dump_callback(d->ctx, d->product, RAWSPEC_CALLBACK_POST_DUMP);
 }
 
+// ----------------------------------------------------------------------------
+// Memory.  Device buffers come from the device's stream-ordered memory pool
+// (cudaMallocAsync on the context stream, freed with cudaFreeAsync), which
+// keeps freed memory for later contexts and never synchronises the device, so
+// that creating and freeing contexts does not stall other contexts' work (a
+// job server runs many).  Page-locked host buffers (h_pwrbuf, h_icsbuf, the
+// library's host blocks) are likewise kept by size class for later contexts:
+// pinning memory costs milliseconds per allocation.
+// ----------------------------------------------------------------------------
+void keep_pool_memory(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> g(mu);
+  if (std::find(done.begin(), done.end(), device) != done.end()) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool (this process's memory only)
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
+  done.push_back(device);
+}
+
+std::mutex g_pin_mu;
+std::multimap<size_t, void*> g_pin_cache;  // size class -> buffer
+size_t g_pin_cached = 0;
+constexpr size_t kPinCacheCap = size_t(8) << 30;
+
+// Allocation size of a pinned request: a multiple of a quarter of the
+// largest power of two not above it (at most 25 % more), 4 KiB at least.
+size_t pin_class(size_t bytes) {
+  if (bytes <= 4096) return 4096;
+  size_t p = 1;
+  while (p * 2 <= bytes) p *= 2;
+  const size_t q = p / 4;
+  return (bytes + q - 1) / q * q;
+}
+
+cudaError_t pinned_alloc(void** ptr, size_t bytes) {
+  const size_t c = pin_class(bytes);
+  {
+    std::lock_guard<std::mutex> g(g_pin_mu);
+    auto it = g_pin_cache.find(c);
+    if (it != g_pin_cache.end()) {
+      *ptr = it->second;
+      g_pin_cache.erase(it);
+      g_pin_cached -= c;
+      return cudaSuccess;
+    }
+  }
+  return cudaHostAlloc(ptr, c, cudaHostAllocDefault);
+}
+
+// The buffer must no longer be used by any stream.
+void pinned_free(void* ptr, size_t bytes) {
+  if (!ptr) return;
+  const size_t c = pin_class(bytes);
+  {
+    std::lock_guard<std::mutex> g(g_pin_mu);
+    if (g_pin_cached + c <= kPinCacheCap) {
+      g_pin_cache.emplace(c, ptr);
+      g_pin_cached += c;
+      return;
+    }
+  }
+  cudaFreeHost(ptr);
+}
+
 template <typename T>
 int dev_alloc(GpuCtx* g, T** p, size_t bytes) {
   if (bytes == 0) {
@@ -373,7 +443,7 @@ int dev_alloc(GpuCtx* g, T** p, size_t bytes) {
     return 0;
   }
   void* v = nullptr;
-  cudaError_t e = cudaMalloc(&v, bytes);
+  cudaError_t e = cudaMallocAsync(&v, bytes, g->stream);
   if (e != cudaSuccess) {
     fprintf(stderr, "got error %s allocating %zu bytes of device memory\n", cudaGetErrorName(e), bytes);
     fflush(stderr);
@@ -702,6 +772,7 @@ int rawspec_initialize(rawspec_context* ctx) {
     }                                                                                              \
   } while (0)
 
+  keep_pool_memory(g->device);
   CK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
   for (int k = 0; k < kMaxCopyGroups; k++) CK(cudaEventCreateWithFlags(&g->ev_ready[k], cudaEventDisableTiming));
@@ -721,7 +792,7 @@ int rawspec_initialize(rawspec_context* ctx) {
     ctx->h_blkbufs = (char**)calloc(ctx->Nb_host, sizeof(char*));
     if (!ctx->h_blkbufs) FAIL();
     for (unsigned i = 0; i < ctx->Nb_host; i++)
-      CK(cudaHostAlloc((void**)&ctx->h_blkbufs[i], blk_bytes, cudaHostAllocDefault));
+      CK(pinned_alloc((void**)&ctx->h_blkbufs[i], blk_bytes));
   } else {
     g->caller_managed = true;
     g->locked_here.assign(ctx->Nb_host, 0);
@@ -774,13 +845,13 @@ int rawspec_initialize(rawspec_context* ctx) {
     const int M = (int)(P.Nis > 1 ? P.Nss : P.Na);
     const int upc = (int)(P.Nis > 1 ? 1 : P.Nss / P.Na);
 
-    CK(cudaHostAlloc((void**)&ctx->h_pwrbuf[i], ctx->h_pwrbuf_size[i], cudaHostAllocDefault));
+    CK(pinned_alloc((void**)&ctx->h_pwrbuf[i], ctx->h_pwrbuf_size[i]));
     P.out_bytes = ctx->h_pwrbuf_size[i];
     if (dev_alloc(g, &P.d_out, P.out_bytes)) FAIL();
     CK(cudaMemsetAsync(P.d_out, 0, P.out_bytes, g->stream));
     if (ctx->incoherently_sum) {
       P.ics_bytes = ctx->h_pwrbuf_size[i] / ctx->Nant;
-      CK(cudaHostAlloc((void**)&ctx->h_icsbuf[i], P.ics_bytes, cudaHostAllocDefault));
+      CK(pinned_alloc((void**)&ctx->h_icsbuf[i], P.ics_bytes));
       if (dev_alloc(g, &P.d_ics, P.ics_bytes)) FAIL();
       CK(cudaMemsetAsync(P.d_ics, 0, P.ics_bytes, g->stream));
     }
@@ -812,7 +883,7 @@ int rawspec_initialize(rawspec_context* ctx) {
       L.tab = P.d_tw;
       if (dev_alloc(g, &P.d_ctl, sizeof(int))) FAIL();
       CK(cudaMemsetAsync(P.d_ctl, 0, sizeof(int), g->stream));
-      CK(cudaHostAlloc((void**)&P.h_err, sizeof(int), cudaHostAllocDefault));
+      CK(pinned_alloc((void**)&P.h_err, sizeof(int)));
       *P.h_err = 0;
       L.err = P.d_ctl;
     } else if (!P.large) {
@@ -872,7 +943,7 @@ int rawspec_initialize(rawspec_context* ctx) {
         const size_t nctl = (size_t)large_fused_ctl_ints(L);
         if (dev_alloc(g, &P.d_ctl, nctl * sizeof(int))) FAIL();
         CK(cudaMemsetAsync(P.d_ctl, 0, nctl * sizeof(int), g->stream));
-        CK(cudaHostAlloc((void**)&P.h_err, sizeof(int), cudaHostAllocDefault));
+        CK(pinned_alloc((void**)&P.h_err, sizeof(int)));
         *P.h_err = 0;
         L.ctl = P.d_ctl;
       }
@@ -921,55 +992,60 @@ int rawspec_initialize(rawspec_context* ctx) {
 }
 
 void rawspec_cleanup(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  // nothing may still use the buffers: every stream of the context drains first
+  if (g) {
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->copy_stream) cudaStreamSynchronize(g->copy_stream);
+    for (int i = 0; i < MAX_OUTPUTS; i++)
+      if (g->prod[i].own_stream) cudaStreamSynchronize(g->prod[i].own_stream);
+  }
   for (int i = 0; i < MAX_OUTPUTS; i++) {
     if (ctx->h_pwrbuf[i]) {
-      cudaFreeHost(ctx->h_pwrbuf[i]);
+      pinned_free(ctx->h_pwrbuf[i], ctx->h_pwrbuf_size[i]);
       ctx->h_pwrbuf[i] = nullptr;
     }
     if (ctx->h_icsbuf[i]) {
-      cudaFreeHost(ctx->h_icsbuf[i]);
+      pinned_free(ctx->h_icsbuf[i], g ? g->prod[i].ics_bytes : ctx->h_pwrbuf_size[i] / std::max(1u, ctx->Nant));
       ctx->h_icsbuf[i] = nullptr;
     }
   }
-  GpuCtx* g = G(ctx);
   if (!g) return;
-  if (g->stream) cudaStreamSynchronize(g->stream);
+  const size_t blk_bytes = (size_t)ctx->Ntpb * ctx->Np * ctx->Nc * 2 * (ctx->Nbps / 8);
   if (g->caller_managed) {
     for (unsigned i = 0; i < g->registered; i++)
       if (g->locked_here[i]) cudaHostUnregister(ctx->h_blkbufs[i]);
   } else if (ctx->h_blkbufs) {
     for (unsigned i = 0; i < ctx->Nb_host; i++)
-      if (ctx->h_blkbufs[i]) cudaFreeHost(ctx->h_blkbufs[i]);
+      if (ctx->h_blkbufs[i]) pinned_free(ctx->h_blkbufs[i], blk_bytes);
     free(ctx->h_blkbufs);
     ctx->h_blkbufs = nullptr;
   }
-  cudaFree(g->d_in);
-  cudaFree(g->d_in4);
-  cudaFree(g->d_aws);
+  auto dfree = [&](void* p) {
+    if (p) cudaFreeAsync(p, g->stream);
+  };
+  dfree(g->d_in);
+  dfree(g->d_in4);
+  dfree(g->d_aws);
   for (int i = 0; i < MAX_OUTPUTS; i++) {
-    cudaFree(g->prod[i].d_out);
-    cudaFree(g->prod[i].d_ics);
-    cudaFree(g->prod[i].d_tw);
-    cudaFree(g->prod[i].d_ctl);
-    if (g->prod[i].h_err) cudaFreeHost(g->prod[i].h_err);
-    cudaFree(g->prod[i].d_partial);
-    cudaFree(g->prod[i].d_scratch);
-    if (g->prod[i].own_stream) {
-      cudaStreamSynchronize(g->prod[i].own_stream);
-      cudaStreamDestroy(g->prod[i].own_stream);
-    }
+    dfree(g->prod[i].d_out);
+    dfree(g->prod[i].d_ics);
+    dfree(g->prod[i].d_tw);
+    dfree(g->prod[i].d_ctl);
+    pinned_free(g->prod[i].h_err, sizeof(int));
+    dfree(g->prod[i].d_partial);
+    dfree(g->prod[i].d_scratch);
+    if (g->prod[i].own_stream) cudaStreamDestroy(g->prod[i].own_stream);
     if (g->prod[i].ev_join) cudaEventDestroy(g->prod[i].ev_join);
   }
+  if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   for (auto& p : g->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
   }
   for (auto e : g->free_events) cudaEventDestroy(e);
-  if (g->copy_stream) {
-    cudaStreamSynchronize(g->copy_stream);
-    cudaStreamDestroy(g->copy_stream);
-  }
+  if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
   for (int k = 0; k < kMaxCopyGroups; k++)
     if (g->ev_ready[k]) cudaEventDestroy(g->ev_ready[k]);
   if (g->ev_free) cudaEventDestroy(g->ev_free);
