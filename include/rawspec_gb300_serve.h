@@ -55,8 +55,10 @@ int rawspec_gb300_server_submit(rawspec_gb300_server *s, const rawspec_context *
 
 /* Queues one input buffer of a job: Nb blocks of Nc * Ntpb * Np * 2 * Nbps / 8
  * bytes each, in block order (4-bit input: the packed bytes, half that size).
- * The data are copied.  0, or 1 (unknown or closed job, wrong size, time-out
- * of 60 s waiting for queue space). */
+ * The data are copied into one of the job's max_queued page-locked slots,
+ * which exist once the job is admitted: a push to a pending job, or to a job
+ * whose slots are all queued, waits.  0, or 1 (unknown or closed job, wrong
+ * size, time-out of 60 s waiting for a slot). */
 int rawspec_gb300_server_push(rawspec_gb300_server *s, int job, const void *data, size_t bytes);
 
 /* No more buffers for the job: once its queue is processed, the job waits

@@ -14,7 +14,8 @@
 // others run starts as soon as it fits.
 //
 // Pushed buffers are copied by the pushing thread into the job's pool of
-// pinned host slots, which are the context's host blocks (caller-managed):
+// pinned host slots (allocated when the job is admitted; a push to a pending
+// job waits for them), which are the context's host blocks (caller-managed):
 // the loop points the context's block pointers at the slot of the buffer for
 // the call, so the request loop copies no data itself.  Slots return to a
 // server-wide cache of pinned buffers when their job ends, so that jobs do
@@ -181,8 +182,27 @@ void request_loop(rawspec_gb300_server* s) {
       s->used += j->est;
       s->peak_active = std::max(s->peak_active, s->active);
       lk.unlock();
-      const int rc = rawspec_initialize(&j->ctx);
+      // the job's pinned slots, which are also the context's host blocks
+      // (already page-locked, so the library uses them as they are); the
+      // loop points the block pointers at each buffer's slot
+      int rc = 0;
+      std::vector<std::pair<char*, size_t>> pool;
+      for (int k = 0; k < s->max_queued && rc == 0; k++) {
+        size_t cap = 0;
+        char* p = take_pinned(s, j->blk_bytes * j->ctx.Nb, &cap);
+        if (p) pool.emplace_back(p, cap);
+        else rc = 1;
+      }
+      if (rc == 0) {
+        j->blocks.resize(j->ctx.Nb);
+        for (unsigned b = 0; b < j->ctx.Nb; b++) j->blocks[b] = pool[0].first + b * j->blk_bytes;
+        j->ctx.h_blkbufs = j->blocks.data();
+        j->ctx.Nb_host = j->ctx.Nb;
+        rc = rawspec_initialize(&j->ctx);
+      }
       lk.lock();
+      j->pool = pool;
+      for (auto& pc : pool) j->free_slots.push_back(pc.first);
       if (rc) {
         free_pool(s, j);
         retire(s, j, RAWSPEC_GB300_JOB_FAILED);
@@ -323,28 +343,9 @@ int rawspec_gb300_server_submit(rawspec_gb300_server* s, const rawspec_context* 
   j->user = user;
   c.dump_callback = job_dump_cb;
   c.user_data = j.get();
-  for (int k = 0; k < s->max_queued; k++) {
-    size_t cap = 0;
-    char* p = take_pinned(s, j->blk_bytes * v.Nb, &cap);
-    if (!p) {
-      free_pool(s, j.get());
-      return -1;
-    }
-    j->pool.emplace_back(p, cap);
-    j->free_slots.push_back(p);
-  }
-  // the context's host blocks are the slots (already page-locked, so the
-  // library uses them as they are); the loop points them at each buffer
-  j->blocks.resize(v.Nb);
-  for (unsigned b = 0; b < v.Nb; b++) j->blocks[b] = j->pool[0].first + b * j->blk_bytes;
-  c.h_blkbufs = j->blocks.data();
-  c.Nb_host = v.Nb;
   j->t_submit = now_s();
   std::lock_guard<std::mutex> g(s->mu);
-  if (s->stop) {
-    free_pool(s, j.get());
-    return -1;
-  }
+  if (s->stop) return -1;
   const int id = s->next_id++;
   j->id = id;
   s->jobs[id] = std::move(j);
