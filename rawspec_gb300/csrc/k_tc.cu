@@ -52,8 +52,8 @@ struct TcCfg {
   static constexpr int B_BYTES = (ND / 8) * SBO;
   static constexpr int TW_BYTES = N * 8;      // W_N^(n2 k1) as [k1][n2] float2
   static constexpr int TAB_BYTES = B_BYTES + TW_BYTES;
-  // stage-1 operand | T hi | T lo | DFT operand | twiddles | 4 mbarriers, tensor-memory slot, abort flag
-  static constexpr int SMEM = 3 * A_BYTES + TAB_BYTES + 48;
+  // stage-1 operand | T hi | T lo | DFT operand | twiddles | 2 mbarriers, tensor-memory slot
+  static constexpr int SMEM = 3 * A_BYTES + TAB_BYTES + 32;
   static constexpr int TMEM_COLS = 2 * ND;    // stage-1 and stage-2 accumulators
   static constexpr int THREADS = 256;         // two warps per tensor-memory lane quarter
   static constexpr int MINB = S == 16 ? 3 : 512 / TMEM_COLS;
@@ -84,11 +84,7 @@ __device__ __forceinline__ uint32_t codes_to_h2(uint32_t x, uint32_t sel) {
 // tensor-memory columns and its own mbarrier; every shared-memory operand is
 // rewritten only after the MMAs reading it have completed.  Warps w and w + 4
 // read the same tensor-memory lanes and split the accumulator columns
-// between them (8-column chunks q with q % 2 = w / 4).  Within a tile no
-// thread waits for the others at a barrier: each arrives on an mbarrier once
-// its part of an operand is written (and its reads of the accumulator that
-// the next MMAs overwrite are complete), and only the issuing thread waits
-// for all 256 arrivals before it issues the MMAs.
+// between them (8-column chunks q with q % 2 = w / 4).
 template <int S, int POL>
 __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const __grid_constant__ TcLaunch a) {
   using C = TcCfg<S>;
@@ -104,12 +100,9 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
   unsigned char* sAlo = sm + 2 * C::A_BYTES; // T lo
   unsigned char* sB = sm + 3 * C::A_BYTES;   // DFT operand [hi | lo], then the twiddles
   const float2* sTw = reinterpret_cast<const float2*>(sB + C::B_BYTES);
-  uint64_t* mb1 = reinterpret_cast<uint64_t*>(sB + C::TAB_BYTES);  // stage-1 MMAs complete
-  uint64_t* mb2 = mb1 + 1;                                          // stage-2 MMAs complete
-  uint64_t* mbA = mb1 + 2;                                          // stage-1 operand written
-  uint64_t* mbT = mb1 + 3;                                          // stage-2 operand written
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mb1 + 4);
-  volatile int* s_abort = reinterpret_cast<volatile int*>(tslot + 1);
+  uint64_t* mb1 = reinterpret_cast<uint64_t*>(sB + C::TAB_BYTES);
+  uint64_t* mb2 = mb1 + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mb1 + 2);
   float* red = reinterpret_cast<float*>(sm);  // reduction area over the operands
 
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -121,9 +114,6 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
   if (tid == 0) {
     tc::mbar_init(mb1, 1);
     tc::mbar_init(mb2, 1);
-    tc::mbar_init(mbA, T);
-    tc::mbar_init(mbT, T);
-    *s_abort = 0;
   }
   if (warp == 0) {
     tc::tmem_alloc(tslot, C::TMEM_COLS);
@@ -138,8 +128,8 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
   const int half = warp >> 2;                                        // its column chunks
   const uint32_t aA1 = tc::smem_u32(sA1), aHi = tc::smem_u32(sAhi), aLo = tc::smem_u32(sAlo);
   const uint32_t bF = tc::smem_u32(sB);
-  unsigned ph1 = 0, ph2 = 0, phA = 0, phT = 0;
-  int bad = 0;  // one of this thread's waits timed out (or gave up after another's)
+  unsigned ph1 = 0, ph2 = 0;
+  int bad = 0;  // one of this thread's waits timed out
 
   // input words: thread -> (spectrum of the tile, n2), a quarter of the n1 range
   const int pair = tid & 63, lsp = pair / S, ln2 = pair % S, n1_0 = (tid >> 6) * (S / 4);
@@ -172,15 +162,13 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
           make_uint4(h1[0], h1[1], h1[2], h1[3]);
     }
   };
-  auto fail = [&]() {
-    bad = 1;
-    *s_abort = 1;
-  };
-  // this thread's operand writes and its earlier tensor-memory loads are complete
-  auto ready = [&](uint64_t* mb) {
+  // operands written and earlier tensor-memory loads complete -> MMAs
+  auto sync_for_mma = [&]() -> bool {
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
-    tc::mbar_arrive(mb);
+    const int stop = __syncthreads_or(bad);
+    if (!stop && tid == 0) tc::fence_after_sync();
+    return stop != 0;
   };
   auto issue_s1 = [&]() {
 #pragma unroll
@@ -201,20 +189,8 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
                   tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC_HI, 1u);
     tc::mma_commit(mb2);
   };
-  // the issuing thread: all threads ready -> the stage's MMAs
-  auto issue = [&](uint64_t* mb, unsigned& ph, bool stage1) {
-    if (tid != 0) return;
-    const bool ok = tc::mbar_wait_abortable(mb, ph, kTcWaitCycles, s_abort);
-    ph ^= 1;
-    if (!ok) {
-      fail();
-      return;
-    }
-    tc::fence_after_sync();
-    if (stage1) issue_s1(); else issue_s2();
-  };
   auto wait = [&](uint64_t* mb, unsigned& ph) {
-    if (!tc::mbar_wait_abortable(mb, ph, kTcWaitCycles, s_abort)) fail();
+    if (!tc::mbar_wait_bounded(mb, ph, kTcWaitCycles)) bad = 1;
     ph ^= 1;
     tc::fence_after_sync();
   };
@@ -317,12 +293,12 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
     load(src);
     convert();
     if (ntiles > 1) load(src + tile_words);
-    ready(mbA);
-    issue(mbA, phA, true);
+    if ((stop = sync_for_mma())) break;
+    if (tid == 0) issue_s1();
     wait(mb1, ph1);
     epi1();
-    ready(mbT);
-    issue(mbT, phT, false);
+    if ((stop = sync_for_mma())) break;
+    if (tid == 0) issue_s2();
 
     for (int t = 0; t < ntiles; ++t) {
       const bool more = t + 1 < ntiles;
@@ -330,19 +306,19 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
         // the stage-1 MMAs of tile t have completed: their operand is free
         convert();
         if (t + 2 < ntiles) load(src + (t + 2) * tile_words);
-        ready(mbA);
-        issue(mbA, phA, true);
+        if ((stop = sync_for_mma())) break;
+        if (tid == 0) issue_s1();
       }
-      // the stage-2 MMAs of tile t have completed: T hi / lo are free
       wait(mb2, ph2);
       epi2(acc);
       if (more) {
         wait(mb1, ph1);
         epi1();
-        ready(mbT);
-        issue(mbT, phT, false);
+        if ((stop = sync_for_mma())) break;
+        if (tid == 0) issue_s2();
       }
     }
+    if (stop) break;
 
     // ---- the unit's (chunk's) spectrum: fixed-order sum over the tile's sequences
     if ((stop = __syncthreads_or(bad) != 0)) break;

@@ -105,22 +105,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mb, unsigned parity,
   return true;
 }
 
-// One arrival of this thread (release: its earlier writes are visible to a
-// thread that then observes the phase complete).
-__device__ __forceinline__ void mbar_arrive(uint64_t* mb) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mb)) : "memory");
-}
-// As mbar_wait_bounded, and gives up at once when *abort is set (another
-// thread of the CTA timed out).
-__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* mb, unsigned parity, long long limit,
-                                                    volatile int* abort) {
-  if (mbar_try_wait(mb, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(mb, parity))
-    if (*abort || clock64() - t0 > limit) return false;
-  return true;
-}
-
 // ---- tensor memory -> registers ----
 // Two loads of 16 consecutive columns of this thread's lane (32x32b shape),
 // then the wait; the registers are tied to the wait so that no use of them
