@@ -135,6 +135,7 @@ struct LargeLaunch {
   int unit0 = 0, unit_count = 0;  // units of this launch (two-kernel path)
   int ring = 0;                   // intermediate slots
   int lag = 2;                    // row tiles of slab s follow the column tiles of slab s + lag
+  int lag_pipe = 2;               // the lag of a launch over one channel group of the pipelined call
   int* ctl = nullptr;             // [0] error, [1] CTAs finished, [2] item counter, [3..3+S) A done, [3+S..3+2S) B done
   int fused_ctas = 0;             // persistent grid size
   // fused kernel: tensor maps of the input (rows of N1 words), of the

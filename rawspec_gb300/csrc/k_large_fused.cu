@@ -34,6 +34,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "detect.cuh"
 #include "fft_core.cuh"
@@ -732,6 +733,8 @@ cudaError_t large_fused_plan(LargeLaunch& L) {
 #else
   L.ring = std::max(L.lag + 2, L.lag + d);
 #endif
+  L.lag_pipe = L.lag;
+  if (const char* v = getenv("RAWSPEC_GB300_FUSED_LAG_PIPE")) L.lag_pipe = std::max(1, std::min(L.ring - 1, atoi(v)));
   return L.ring > L.lag ? cudaSuccess : cudaErrorInvalidValue;
 }
 

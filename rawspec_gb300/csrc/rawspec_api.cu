@@ -525,6 +525,7 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
     L.S = (c1 - c0) * L.Nss;
     L.unit0 = c0 * L.units_per_chan;
     L.unit_count = (c1 - c0) * L.units_per_chan;
+    if (c1 - c0 < (int)ctx->Nc) L.lag = L.lag_pipe;  // a channel group: its own lag
     if (P.fused) {
       {
         ProfScope ps(g, RAWSPEC_GB300_K_LARGE_FUSED, P.stream);
