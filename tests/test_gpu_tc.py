@@ -18,7 +18,7 @@ import pytest
 from cases import derived_nb
 from oracle import oracle as O
 from rawspec_gb300 import api, synth
-from util import REL_TOL, normalized_error
+from util import REL_TOL, normalized_error, rms_normalized_error
 
 pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
@@ -160,3 +160,28 @@ def test_tensor_dft_equals_plain_path_at_production_shape(cuda_device, monkeypat
     got_cc, n_tc2, n_small = run_tc(monkeypatch, c, blocks, tensor=False)
     assert n_tc > 0 and n_tc2 == 0 and n_small > 0
     assert normalized_error(got_tc[0], got_cc[0], 1, Nc, 1024) < 2 * REL_TOL
+
+
+@pytest.mark.parametrize("npol", [1, 4])
+def test_mixed_precision_products_error_report(cuda_device, monkeypatch, npol):
+    # the mixed-precision configuration: Gaussian int8 voltages (sigma 16,
+    # one tone), products Nfft 8/256/1024/4096 with Nint 128/256/512/3072,
+    # on the tensor-core DFT where it applies (256, 1024, 4096 total power)
+    # and on the CUDA-core kernels; max and RMS error per product against
+    # the FP64 oracle.  Two channels and 192 blocks of 65536 samples, so
+    # that the 3072 x 4096-point integration completes.
+    Nc, Ntpb, nblocks = 2, 1 << 16, 192
+    prods = [(8, 128, npol), (256, 256, npol), (1024, 512, npol), (4096, 3072, npol)]
+    blocks = synth.gaussian_blocks(nblocks, Nc, Ntpb, 2, sigma=16.0, seed=31, tone=(1, 0.3, 8.0))
+    c = dict(Nc=Nc, Np=2, Ntpb=Ntpb, nbits=8, nblocks=nblocks, products=prods, conj=0, fft_dir=1)
+    ref = oracle_for(c, blocks)
+    got_tc, n_tc, _ = run_tc(monkeypatch, c, blocks)
+    got_cc, n_tc0, _ = run_tc(monkeypatch, c, blocks, tensor=False)
+    assert n_tc > 0 and n_tc0 == 0
+    for i, (nt, na, _) in enumerate(prods):
+        assert got_tc[i].shape == ref[i].shape and got_tc[i].size > 0
+        e = {k: (normalized_error(g[i], ref[i], npol, Nc, nt), rms_normalized_error(g[i], ref[i], npol, Nc, nt))
+             for k, g in (("tensor", got_tc), ("fp32", got_cc))}
+        print(f"Nfft {nt} Nint {na} Npolout {npol}: tensor-core path max {e['tensor'][0]:.2e} rms "
+              f"{e['tensor'][1]:.2e}; CUDA-core path max {e['fp32'][0]:.2e} rms {e['fp32'][1]:.2e}")
+        assert e["tensor"][0] < REL_TOL and e["fp32"][0] < REL_TOL, (nt, e)

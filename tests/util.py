@@ -36,6 +36,16 @@ def normalized_error(got: np.ndarray, ref: np.ndarray, npol: int, Nc: int, Nt: i
     return float(np.max(np.abs(g - r) / den))
 
 
+def rms_normalized_error(got: np.ndarray, ref: np.ndarray, npol: int, Nc: int, Nt: int) -> float:
+    """Root mean square of the per-bin errors of normalized_error."""
+    g, _ = total_power_planes(np.asarray(got, np.float64), npol, Nc, Nt)
+    r, tp = total_power_planes(np.asarray(ref, np.float64), npol, Nc, Nt)
+    mean = tp.mean(axis=-1, keepdims=True)
+    den = np.maximum(np.abs(tp), 1e-2 * np.abs(mean))
+    den = np.where(den > 0, den, 1.0)
+    return float(np.sqrt(np.mean(((g - r) / den) ** 2)))
+
+
 def load_golden(name: str) -> dict:
     with np.load(GOLDEN / f"{name}.npz") as z:
         return {k: z[k] for k in z.files}
