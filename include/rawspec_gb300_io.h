@@ -150,6 +150,11 @@ typedef struct {
  * Returns the number of bytes, or -1 if cap is too small. */
 long rawspec_gb300_fil_header(const rawspec_gb300_fil_hdr *hdr, void *buf, size_t cap);
 
+/* The same header padded to at least minlen bytes with blank "rawdatafile"
+ * entries ahead of the real one (rawspec_fbutils.c:330-404); minlen 0: no
+ * padding. */
+long rawspec_gb300_fil_header_padded(const rawspec_gb300_fil_hdr *hdr, void *buf, size_t cap, int minlen);
+
 /* SIGPROC telescope_id of a telescope name, -1 if unknown
  * (rawspec_fbutils.c:533-576). */
 int rawspec_gb300_telescope_id(const char *name);
@@ -187,6 +192,47 @@ int rawspec_gb300_fil_writer_close(rawspec_gb300_fil_writer *w);
  * file I/O overlaps the next buffer's processing (rawspec_file.c:102-243).
  * A failed write sets ctx->exit_soon. */
 void rawspec_gb300_fil_dump_callback(rawspec_context *ctx, int output_product, int callback_type);
+
+/* ---------------------------------------------------------------------------
+ * UDP output of the dumps (rawspec_socket.c:21-354)
+ * ------------------------------------------------------------------------- */
+
+/* A UDP socket connected to host:port (IPv4), with the don't-fragment probe
+ * option; -1 if the address cannot be resolved or connected, or if the path's
+ * MTU is below 8600 bytes (the packets carry up to 8 KiB of data). */
+int rawspec_gb300_net_open(const char *host, const char *port);
+
+/* Output rates of the products, total_gbps shared in proportion to their data
+ * volume, i.e. to 1/Nas[i] (rawspec.c:884-901). */
+void rawspec_gb300_net_rates(const rawspec_context *ctx, double total_gbps, double *rates_gbps);
+
+/* One output product's UDP sender: each dump is cut into packets of at most
+ * 2048 floats (whole spectra when a spectrum has fewer channels), each
+ * behind a SIGPROC header of its own channel count, first channel frequency
+ * and start time, padded so that the data start on a 512-byte boundary of a
+ * packet-socket frame (whose UDP payload begins 0x6c bytes in); packets are
+ * paced to rate_gbps.  The dump is sent from the start of h_pwrbuf as Nds
+ * spectra of hdr->nchans floats, as the reference does. */
+typedef struct rawspec_gb300_net_writer rawspec_gb300_net_writer;
+rawspec_gb300_net_writer *rawspec_gb300_net_writer_open(const rawspec_context *ctx, int product,
+                                                        const rawspec_gb300_fil_hdr *hdr, int fd,
+                                                        double rate_gbps);
+
+typedef struct {
+  long long dumps, spectra, packets, bytes, error_packets;
+  double seconds;  /* time spent sending, pacing included */
+} rawspec_gb300_net_stats;
+
+int rawspec_gb300_net_writer_stats(rawspec_gb300_net_writer *w, rawspec_gb300_net_stats *st);
+
+/* Waits for a dump being sent and frees the writer (the socket stays open);
+ * 0, or 1 if packets could not be sent. */
+int rawspec_gb300_net_writer_close(rawspec_gb300_net_writer *w);
+
+/* Dump callback (ctx->user_data: array of writer pointers by product):
+ * PRE_DUMP waits for the product's previous dump to be sent, POST_DUMP starts
+ * a sender thread for this one (rawspec_socket.c:327-354). */
+void rawspec_gb300_net_dump_callback(rawspec_context *ctx, int output_product, int callback_type);
 
 #ifdef __cplusplus
 }

@@ -74,6 +74,15 @@ static double to_dms(double x) {
 }
 
 RSG_EXPORT long rawspec_gb300_fil_header(const rawspec_gb300_fil_hdr *h, void *buf, size_t cap) {
+  return rawspec_gb300_fil_header_padded(h, buf, cap, 0);
+}
+
+/* The header, padded to at least minlen bytes by extra "rawdatafile" entries
+ * of blanks placed before the real one (the later entry wins in a reader):
+ * whole 79-byte entries while more than 98 bytes are missing, then one entry
+ * of the remaining length if it exceeds 19 bytes (rawspec_fbutils.c:330-404). */
+RSG_EXPORT long rawspec_gb300_fil_header_padded(const rawspec_gb300_fil_hdr *h, void *buf, size_t cap,
+                                                int minlen) {
   Sink s = {(unsigned char *)buf, (unsigned char *)buf + cap, 0};
   put_str(&s, "HEADER_START");
   put_str(&s, "machine_id");
@@ -118,6 +127,24 @@ RSG_EXPORT long rawspec_gb300_fil_header(const rawspec_gb300_fil_hdr *h, void *b
   }
   put_str(&s, "source_name");
   put_str(&s, h->source_name);
+  /* bytes still missing once the rawdatafile entry and HEADER_END are added */
+  long pad = (long)minlen - (long)(s.p - (unsigned char *)buf) - (8 + 11 + (long)strnlen(h->rawdatafile, 80)) -
+             (4 + 10);
+  char blanks[80];
+  memset(blanks, ' ', sizeof(blanks) - 1);
+  blanks[sizeof(blanks) - 1] = '\0';
+  while (pad > 98) {
+    blanks[60] = '\0';  /* 4 + 11 + 4 + 60 = 79 bytes */
+    put_str(&s, "rawdatafile");
+    put_str(&s, blanks);
+    pad -= 79;
+  }
+  if (pad > 19) {
+    blanks[60] = ' ';
+    blanks[pad - 19] = '\0';
+    put_str(&s, "rawdatafile");
+    put_str(&s, blanks);
+  }
   put_str(&s, "rawdatafile");
   put_str(&s, h->rawdatafile);
   put_str(&s, "HEADER_END");

@@ -68,6 +68,11 @@ class FilHeader(C.Structure):
     ]
 
 
+class NetStats(C.Structure):
+    _fields_ = [("dumps", C.c_longlong), ("spectra", C.c_longlong), ("packets", C.c_longlong),
+                ("bytes", C.c_longlong), ("error_packets", C.c_longlong), ("seconds", C.c_double)]
+
+
 _declared = False
 
 
@@ -99,6 +104,13 @@ def lib() -> C.CDLL:
                                                            C.c_char_p, C.c_int, C.c_int, C.c_char_p]),
             "rawspec_gb300_fil_writer_close": (C.c_int, [C.c_void_p]),
             "rawspec_gb300_fil_dump_callback": (None, [P, C.c_int, C.c_int]),
+            "rawspec_gb300_fil_header_padded": (C.c_long, [C.POINTER(FilHeader), C.c_void_p, C.c_size_t, C.c_int]),
+            "rawspec_gb300_net_open": (C.c_int, [C.c_char_p, C.c_char_p]),
+            "rawspec_gb300_net_rates": (None, [P, C.c_double, C.POINTER(C.c_double)]),
+            "rawspec_gb300_net_writer_open": (C.c_void_p, [P, C.c_int, C.POINTER(FilHeader), C.c_int, C.c_double]),
+            "rawspec_gb300_net_writer_stats": (C.c_int, [C.c_void_p, C.POINTER(NetStats)]),
+            "rawspec_gb300_net_writer_close": (C.c_int, [C.c_void_p]),
+            "rawspec_gb300_net_dump_callback": (None, [P, C.c_int, C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -114,9 +126,9 @@ def parse_header(text: bytes) -> RawHeader:
     return h
 
 
-def fil_header_bytes(h: FilHeader) -> bytes:
+def fil_header_bytes(h: FilHeader, minlen: int = 0) -> bytes:
     buf = C.create_string_buffer(4096)
-    n = lib().rawspec_gb300_fil_header(C.byref(h), buf, len(buf))
+    n = lib().rawspec_gb300_fil_header_padded(C.byref(h), buf, len(buf), minlen)
     if n < 0:
         raise ValueError("header larger than 4096 bytes")
     return buf.raw[:n]
@@ -164,3 +176,39 @@ def write_raw_file(path: str | Path, blocks: Sequence[np.ndarray], pktidx: Seque
         for b, p in zip(blocks, pktidx):
             f.write(raw_block_header(obsnchan, npol, nbits, ntpb, p, directio=directio, **kw))
             f.write(np.ascontiguousarray(b, dtype=np.uint8).tobytes())  # data follow the header directly
+
+
+# ---------------------------------------------------------------------------
+# SIGPROC header parsing (for checking output)
+# ---------------------------------------------------------------------------
+
+_INT_KEYS = {"machine_id", "telescope_id", "data_type", "nchans", "nbeams", "ibeam", "nbits", "nifs",
+             "barycentric", "pulsarcentric"}
+_STR_KEYS = {"source_name", "rawdatafile"}
+
+
+def parse_fil_header(buf: bytes) -> tuple[dict, int]:
+    """(keyword values, header length) of a SIGPROC header at the start of buf;
+    a repeated keyword keeps its last value."""
+    import struct
+
+    def string(o):
+        n = struct.unpack_from("<i", buf, o)[0]
+        return buf[o + 4:o + 4 + n].decode("latin-1"), o + 4 + n
+
+    kw, o = string(0)
+    if kw != "HEADER_START":
+        raise ValueError("not a SIGPROC header")
+    out = {}
+    while True:
+        kw, o = string(o)
+        if kw == "HEADER_END":
+            return out, o
+        if kw in _INT_KEYS:
+            out[kw] = struct.unpack_from("<i", buf, o)[0]
+            o += 4
+        elif kw in _STR_KEYS:
+            out[kw], o = string(o)
+        else:
+            out[kw] = struct.unpack_from("<d", buf, o)[0]
+            o += 8
