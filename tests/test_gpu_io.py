@@ -132,3 +132,70 @@ def test_ingest_handle_streams_several_stems(cuda_device, tmp_path):
                 np.testing.assert_array_equal(a, b)
     finally:
         spec.close()
+
+
+def test_dumps_over_udp_equal_the_direct_dumps(cuda_device):
+    # the UDP sender as the dump callback of a GPU context: the packets of
+    # every dump, reassembled, equal the dumps of the same buffers collected
+    # directly
+    import socket
+
+    Nc, Ntpb, nbuf = 4, 1 << 15, 4
+    prods = [(1024, 8, 1), (64, 256, 1)]
+    rng = np.random.default_rng(23)
+    blocks = np.clip(np.rint(rng.standard_normal((nbuf, Nc, Ntpb, NP, 2)) * 20), -128, 127).astype(np.int8)
+    host = blocks.view(np.uint8).reshape(nbuf, -1)
+    spec = api.Spectrometer(Nc, NP, Ntpb, 8, prods)
+    try:
+        spec.process(host)
+        want = [[np.array(d) for d in p] for p in spec.dumps]
+    finally:
+        spec.close()
+
+    rx = socket.socket(socket.AF_INET, socket.SOCK_DGRAM)
+    rx.setsockopt(socket.SOL_SOCKET, socket.SO_RCVBUF, 32 << 20)
+    rx.bind(("127.0.0.1", 0))
+    L = io.lib()
+    fd = L.rawspec_gb300_net_open(b"127.0.0.1", str(rx.getsockname()[1]).encode())
+    assert fd >= 0
+    ctx = api.make_context(Nc, NP, Ntpb, 8, prods)
+    assert L.rawspec_initialize(C.byref(ctx)) == 0
+    rates = (C.c_double * len(prods))()
+    L.rawspec_gb300_net_rates(C.byref(ctx), 50.0, rates)
+    writers = []
+    try:
+        for i, (nt, na, npol) in enumerate(prods):
+            h = io.FilHeader()
+            h.nchans, h.nbits, h.nifs, h.fch1, h.foff, h.tsamp = Nc * nt, 32, 1, 1500.0, -0.001, 1e-3 * i + 1e-3
+            h.rawdatafile = f"product{i}".encode()
+            w = L.rawspec_gb300_net_writer_open(C.byref(ctx), i, C.byref(h), fd, rates[i])
+            assert w
+            writers.append(w)
+        arr = (C.c_void_p * len(writers))(*writers)
+        ctx.user_data = C.cast(arr, C.c_void_p)
+        ctx.dump_callback = C.cast(L.rawspec_gb300_net_dump_callback, api.DUMP_CALLBACK)
+        nbytes = Nc * Ntpb * NP * 2
+        for b in range(nbuf):
+            assert L.rawspec_wait_for_completion(C.byref(ctx)) == 0
+            C.memmove(ctx.h_blkbufs[0], host[b].ctypes.data, nbytes)
+            assert L.rawspec_copy_blocks_to_gpu_and_start_processing(C.byref(ctx), 1, 0, 1) == 0
+        assert L.rawspec_wait_for_completion(C.byref(ctx)) == 0
+    finally:
+        for w in writers:
+            assert L.rawspec_gb300_net_writer_close(w) == 0
+        L.rawspec_cleanup(C.byref(ctx))
+        os.close(fd)
+    rx.setblocking(False)
+    got = {i: [] for i in range(len(prods))}
+    while True:
+        try:
+            p = rx.recv(1 << 17)
+        except BlockingIOError:
+            break
+        hdr, hl = io.parse_fil_header(p)
+        got[int(hdr["rawdatafile"][-1])].append(np.frombuffer(p[hl:], dtype=np.float32))
+    rx.close()
+    for i in range(len(prods)):
+        stream = np.concatenate(got[i])
+        assert stream.size == sum(d.size for d in want[i]) > 0
+        np.testing.assert_array_equal(stream, np.concatenate(want[i]))
