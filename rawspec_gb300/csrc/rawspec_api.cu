@@ -120,6 +120,13 @@ struct GpuCtx {
   std::vector<cudaEvent_t> free_events;
   double prof_ms[RAWSPEC_GB300_K_COUNT] = {0};
   unsigned long long prof_n[RAWSPEC_GB300_K_COUNT] = {0};
+  // rawspec_start_processing's work, captured once per pattern (each
+  // product's write/add mode and dump, the direction, callbacks) and replayed
+  struct Graph {
+    cudaGraphExec_t exec;
+    unsigned long long launches;
+  };
+  std::map<unsigned long long, Graph> graphs;
 };
 
 GpuCtx* G(rawspec_context* ctx) { return reinterpret_cast<GpuCtx*>(ctx->gpu_ctx); }
@@ -180,6 +187,14 @@ void collect_profile(GpuCtx* g) {
 // ----------------------------------------------------------------------------
 bool is_pow2(unsigned x) { return x && !(x & (x - 1)); }
 int ilog2u(unsigned x) { int l = 0; while ((1u << l) < x) ++l; return l; }
+
+// rawspec_start_processing replays CUDA graphs of its launches unless
+// RAWSPEC_GB300_GRAPHS=0 (read at each call).
+constexpr size_t kMaxGraphs = 64;
+bool graphs_wanted() {
+  const char* v = getenv("RAWSPEC_GB300_GRAPHS");
+  return !(v && v[0] == '0');
+}
 
 // Which products of 8-bit input run their DFT on the tensor cores (k_tc)
 // rather than in k_small: by default the total-power products of N = 1024,
@@ -1040,6 +1055,8 @@ void rawspec_cleanup(rawspec_context* ctx) {
     if (g->prod[i].ev_join) cudaEventDestroy(g->prod[i].ev_join);
   }
   if (g->stream) cudaStreamSynchronize(g->stream);
+  for (auto& kv : g->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   for (auto& p : g->pending) {
     cudaEventDestroy(p.a);
@@ -1127,7 +1144,46 @@ int rawspec_zero_blocks_to_gpu(rawspec_context* ctx, off_t dst_idx, size_t num_b
 int rawspec_start_processing(rawspec_context* ctx, int fft_dir) {
   GpuCtx* g = G(ctx);
   if (!g) return 1;
-  return process_buffer(ctx, g, fft_dir, 1, nullptr);
+  if (g->profiling || !graphs_wanted()) return process_buffer(ctx, g, fft_dir, 1, nullptr);
+  // the pattern of the buffer about to be processed (inbuf_count + 1)
+  const unsigned next = g->inbuf_count + 1;
+  unsigned long long key = (fft_dir <= 0 ? 1ull : 0ull) | (ctx->dump_callback ? 2ull : 0ull);
+  for (unsigned i = 0; i < ctx->No; i++) {
+    const Product& P = g->prod[i];
+    const unsigned long long m = ((next - 1) % P.Nis == 0 ? 0ull : 1ull) | (next % P.Nis == 0 ? 2ull : 0ull);
+    key |= m << (2 + 2 * i);
+  }
+  auto it = g->graphs.find(key);
+  if (it == g->graphs.end()) {
+    if (g->graphs.size() >= kMaxGraphs) return process_buffer(ctx, g, fft_dir, 1, nullptr);
+    // capture the launches of this pattern (nothing runs while capturing)
+    const unsigned saved_count = g->inbuf_count;
+    const unsigned long long saved_launches = g->launches;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool ok = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      const int rc = process_buffer(ctx, g, fft_dir, 1, nullptr);
+      ok = cudaStreamEndCapture(g->stream, &graph) == cudaSuccess && rc == 0 && graph &&
+           cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    const unsigned long long launches = g->launches - saved_launches;
+    g->inbuf_count = saved_count;
+    g->launches = saved_launches;
+    if (!ok) {
+      cudaGetLastError();
+      if (exec) cudaGraphExecDestroy(exec);
+      g->graphs[key] = GpuCtx::Graph{nullptr, 0};  // this pattern is launched directly from now on
+      return process_buffer(ctx, g, fft_dir, 1, nullptr);
+    }
+    it = g->graphs.emplace(key, GpuCtx::Graph{exec, launches}).first;
+  }
+  if (!it->second.exec) return process_buffer(ctx, g, fft_dir, 1, nullptr);
+  g->inbuf_count++;
+  g->launches += it->second.launches;
+  RSG_CUDA(cudaGraphLaunch(it->second.exec, g->stream));
+  return 0;
 }
 
 // The copy of a full buffer is split into channel groups on a copy stream;

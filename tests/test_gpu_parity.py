@@ -365,3 +365,26 @@ def test_combined_call_pipelines_copy_and_processing(cuda_device, nbits, Nc):
     for i, (nt, na, npol) in enumerate(prods):
         assert got[i].shape == ref[i].shape
         assert normalized_error(got[i], ref[i], npol, Nc, nt) < REL_TOL, (nbits, nt)
+
+
+def test_graph_replay_equals_direct_launches(cuda_device, monkeypatch):
+    # rawspec_start_processing replays a CUDA graph per buffer pattern
+    # (write/add mode and dump of every product); the results and the kernel
+    # launch count equal those of launching the kernels directly
+    Nc, Ntpb, nblocks = 4, 1 << 16, 7
+    prods = [(1 << 17, 1, 1), (1024, 96, 4), (8, 512, -4)]
+    blocks = synth.gaussian_blocks(nblocks, Nc, Ntpb, 2, sigma=20.0, seed=77)
+    out = {}
+    for graphs in ("1", "0"):
+        monkeypatch.setenv("RAWSPEC_GB300_GRAPHS", graphs)
+        spec = api.Spectrometer(Nc, 2, Ntpb, 8, prods, conj=1)
+        try:
+            spec.process(blocks)
+            out[graphs] = ([[np.array(d) for d in p] for p in spec.dumps], spec.events, spec.kernel_launches())
+        finally:
+            spec.close()
+    (d1, e1, n1), (d0, e0, n0) = out["1"], out["0"]
+    assert n1 == n0 > 0 and e1 == e0
+    for p in range(len(prods)):
+        assert len(d1[p]) == len(d0[p]) > 0
+        assert all(np.array_equal(a, b) for a, b in zip(d1[p], d0[p]))
