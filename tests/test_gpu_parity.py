@@ -372,7 +372,7 @@ def test_graph_replay_equals_direct_launches(cuda_device, monkeypatch):
     # (write/add mode and dump of every product); the results and the kernel
     # launch count equal those of launching the kernels directly
     Nc, Ntpb, nblocks = 4, 1 << 16, 7
-    prods = [(1 << 17, 1, 1), (1024, 96, 4), (8, 512, -4)]
+    prods = [(1 << 17, 1, 1), (1024, 256, 4), (8, 512, -4)]
     blocks = synth.gaussian_blocks(nblocks, Nc, Ntpb, 2, sigma=20.0, seed=77)
     out = {}
     for graphs in ("1", "0"):
