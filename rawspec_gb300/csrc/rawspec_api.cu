@@ -188,12 +188,18 @@ void collect_profile(GpuCtx* g) {
 bool is_pow2(unsigned x) { return x && !(x & (x - 1)); }
 int ilog2u(unsigned x) { int l = 0; while ((1u << l) < x) ++l; return l; }
 
-// rawspec_start_processing replays CUDA graphs of its launches unless
-// RAWSPEC_GB300_GRAPHS=0 (read at each call).
+// rawspec_start_processing replays CUDA graphs of its launches for input
+// buffers below 16 MiB, where the host's launch calls take as long as the
+// kernels; larger buffers launch directly (a graph of the production shape's
+// three products measured 2 % slower: its branches start in another order).
+// RAWSPEC_GB300_GRAPHS=1 / =0 (read at each call) selects graphs always /
+// never.
 constexpr size_t kMaxGraphs = 64;
-bool graphs_wanted() {
+bool graphs_wanted(const GpuCtx* g) {
   const char* v = getenv("RAWSPEC_GB300_GRAPHS");
-  return !(v && v[0] == '0');
+  if (v && v[0] == '0') return false;
+  if (v && v[0] == '1') return true;
+  return g->in_bytes < kMinPipelinedBytes;
 }
 
 // Which products of 8-bit input run their DFT on the tensor cores (k_tc)
@@ -1144,7 +1150,7 @@ int rawspec_zero_blocks_to_gpu(rawspec_context* ctx, off_t dst_idx, size_t num_b
 int rawspec_start_processing(rawspec_context* ctx, int fft_dir) {
   GpuCtx* g = G(ctx);
   if (!g) return 1;
-  if (g->profiling || !graphs_wanted()) return process_buffer(ctx, g, fft_dir, 1, nullptr);
+  if (g->profiling || !graphs_wanted(g)) return process_buffer(ctx, g, fft_dir, 1, nullptr);
   // the pattern of the buffer about to be processed (inbuf_count + 1)
   const unsigned next = g->inbuf_count + 1;
   unsigned long long key = (fft_dir <= 0 ? 1ull : 0ull) | (ctx->dump_callback ? 2ull : 0ull);
