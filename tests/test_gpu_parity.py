@@ -384,7 +384,9 @@ def test_graph_replay_equals_direct_launches(cuda_device, monkeypatch):
         finally:
             spec.close()
     (d1, e1, n1), (d0, e0, n0) = out["1"], out["0"]
-    assert n1 == n0 > 0 and e1 == e0
+    # callbacks of one product keep their order; the products' streams interleave freely
+    per_product = lambda ev: [[k for q, k in ev if q == p] for p in range(len(prods))]  # noqa: E731
+    assert n1 == n0 > 0 and per_product(e1) == per_product(e0)
     for p in range(len(prods)):
         assert len(d1[p]) == len(d0[p]) > 0
         assert all(np.array_equal(a, b) for a, b in zip(d1[p], d0[p]))
