@@ -496,25 +496,6 @@ int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int unit0
   return 0;
 }
 
-// Channels [c0, c1) of copy group grp of the pipelined call: equal groups,
-// or, with RAWSPEC_GB300_COPY_TAIL=t (0 < t < Nc / ngroups), a last group of
-// t channels and equal groups before it (less processing remains after the
-// last copy).
-void group_bounds(int Nc, int ngroups, int grp, int* c0, int* c1) {
-  static const int tail = [] {
-    const char* v = getenv("RAWSPEC_GB300_COPY_TAIL");
-    return v ? atoi(v) : 0;
-  }();
-  if (ngroups < 2 || tail <= 0 || tail >= Nc / ngroups) {
-    *c0 = (int)((long long)grp * Nc / ngroups);
-    *c1 = (int)((long long)(grp + 1) * Nc / ngroups);
-    return;
-  }
-  const int head = Nc - tail, hg = ngroups - 1;
-  *c0 = grp < hg ? (int)((long long)grp * head / hg) : head;
-  *c1 = grp < hg ? (int)((long long)(grp + 1) * head / hg) : Nc;
-}
-
 // Queues product i's kernels for the channels [c0, c1) of the buffer.
 int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse, int c0, int c1) {
   Product& P = g->prod[i];
@@ -611,8 +592,8 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
   for (unsigned i = 0; i < ctx->No; i++)
     mode[i] = ((g->inbuf_count - 1) % g->prod[i].Nis == 0) ? ACC_WRITE : ACC_ADD;
   for (int grp = 0; grp < ngroups; grp++) {
-    int c0, c1;
-    group_bounds((int)ctx->Nc, ngroups, grp, &c0, &c1);
+    const int c0 = (int)((long long)grp * ctx->Nc / ngroups);
+    const int c1 = (int)((long long)(grp + 1) * ctx->Nc / ngroups);
     if (c1 <= c0) continue;
     for (unsigned i = 0; i < ctx->No; i++) {
       if (ready) RSG_CUDA(cudaStreamWaitEvent(g->prod[i].stream, ready[grp], 0));
@@ -1238,9 +1219,8 @@ int rawspec_copy_blocks_to_gpu_and_start_processing(rawspec_context* ctx, size_t
   RSG_CUDA(cudaEventRecord(g->ev_free, g->stream));
   RSG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->ev_free, 0));
   for (int grp = 0; grp < ngroups; grp++) {
-    int g0, g1;
-    group_bounds((int)ctx->Nc, ngroups, grp, &g0, &g1);
-    const size_t c0 = (size_t)g0, c1 = (size_t)g1;
+    const size_t c0 = (size_t)grp * ctx->Nc / ngroups;
+    const size_t c1 = (size_t)(grp + 1) * ctx->Nc / ngroups;
     for (size_t b = 0; b < num_blocks; b++) {
       RSG_CUDA(cudaMemcpy2DAsync(dev + c0 * ctx->Nb * row + b * row, ctx->Nb * row, ctx->h_blkbufs[b] + c0 * row, row,
                                  row, c1 - c0, cudaMemcpyHostToDevice, g->copy_stream));
