@@ -61,6 +61,8 @@ struct Job {
   void* user = nullptr;
   int state = RAWSPEC_GB300_JOB_PENDING;
   bool closed = false;
+  int pushing = 0;               // pushes copying into a slot right now (the pool stays theirs)
+  bool release_pending = false;  // the job ended while a push was copying: the last one frees the pool
   std::vector<std::pair<char*, size_t>> pool;  // pinned slots and their capacities
   std::vector<char*> free_slots;
   std::deque<Slot> queue;
@@ -155,6 +157,10 @@ void give_pinned(rawspec_gb300_server* s, char* p, size_t cap) {
 }
 
 void free_pool(rawspec_gb300_server* s, Job* j) {
+  if (j->pushing > 0) {  // a push is copying into one of the slots
+    j->release_pending = true;
+    return;
+  }
   for (auto& pc : j->pool) give_pinned(s, pc.first, pc.second);
   j->pool.clear();
   j->free_slots.clear();
@@ -259,7 +265,7 @@ void request_loop(rawspec_gb300_server* s) {
         }
         j->inflight = true;
         busy = true;
-      } else if (j->closed) {
+      } else if (j->closed && j->pushing == 0) {
         lk.unlock();
         const int rc = rawspec_wait_for_completion(&j->ctx);
         rawspec_cleanup(&j->ctx);
@@ -366,10 +372,19 @@ int rawspec_gb300_server_push(rawspec_gb300_server* s, int job, const void* data
   if (j->state >= RAWSPEC_GB300_JOB_DONE) return 1;
   char* slot = j->free_slots.back();
   j->free_slots.pop_back();
+  j->pushing++;
   lk.unlock();
   memcpy(slot, data, bytes);
   const double t = now_s();
   lk.lock();
+  j->pushing--;
+  if (j->state >= RAWSPEC_GB300_JOB_DONE) {  // the job failed meanwhile
+    if (j->pushing == 0 && j->release_pending) {
+      j->release_pending = false;
+      free_pool(s, j);
+    }
+    return 1;
+  }
   j->queue.push_back(Slot{slot, t});
   s->cv_loop.notify_all();
   return 0;
