@@ -199,13 +199,17 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
 #pragma unroll
     for (int qq = 0; qq < NQ; ++qq) {
       const int q = 2 * qq + half;
+      // the chunk's twiddles are read while its accumulator columns load
+      float2 twv[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) twv[i] = sTw[(8 * q + i) * S + r];
       float h[16], l[16];
       tc::tmem_ld16x2(d1 + lane_off + 16 * q, d1 + lane_off + 2 * S + 16 * q, h, l);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int k1 = 8 * q + i;
         const float2 y = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
-        const float2 tv = cmul(y, sTw[k1 * S + r]);
+        const float2 tv = cmul(y, twv[i]);
         const __half2 hi = __floats2half2_rn(tv.x, tv.y);
         const float2 hf = __half22float2(hi);
         const __half2 lo = __floats2half2_rn(tv.x - hf.x, tv.y - hf.y);
