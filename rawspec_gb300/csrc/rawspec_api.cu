@@ -203,16 +203,18 @@ bool graphs_wanted(const GpuCtx* g) {
 }
 
 // Which products of 8-bit input run their DFT on the tensor cores (k_tc)
-// rather than in k_small: by default the total-power products of N = 1024,
-// where k_tc is at least as fast and overlaps better with the other
-// products' CUDA-core kernels; RAWSPEC_GB300_TENSOR_DFT=1 at initialisation
-// selects it for every case it supports (N = 256, 1024, 4096, all modes up to
-// 1024), =0 for none.
+// rather than in k_small: by default the total-power products of N = 1024
+// and 4096, where k_tc is faster alone (2 % and 13 %) and leaves FMA and
+// issue slots to concurrent CUDA-core kernels; the cross-pol modes stay on
+// k_small (k_tc is as fast alone but slows a mixed step with the fused
+// kernel), N = 256 too (k_tc is slower).  RAWSPEC_GB300_TENSOR_DFT=1 at
+// initialisation selects k_tc for every case it supports (N = 256, 1024,
+// 4096, all modes up to 1024), =0 for none.
 bool tensor_dft_wanted(int logN, int pol) {
   const char* v = getenv("RAWSPEC_GB300_TENSOR_DFT");
   if (v && v[0] == '0') return false;
   if (v && v[0] == '1') return true;
-  return logN == 10 && pol == POL_TP;
+  return (logN == 10 || logN == 12) && pol == POL_TP;
 }
 
 int validate_impl(rawspec_context* ctx, bool* expanded) {
