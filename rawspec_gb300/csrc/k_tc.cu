@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
     }
   };
   auto epi1 = [&]() {
-    if constexpr (POL == POL_TP && NQ == 2) {  // (slower for the cross-pol modes)
+    if constexpr (NQ == 2) {
       // both chunks' twiddles and accumulator columns requested before one wait
       float2 twa[8], twb[8];
 #pragma unroll
