@@ -195,42 +195,7 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
     tc::fence_after_sync();
   };
   // twiddle and hi/lo split: row seq S + k1, columns (n2 = r, re/im)
-  // one chunk of 8 k1 values: twiddle, split, store into T hi / lo
-  auto epi1_chunk = [&](int q, const float (&h)[16], const float (&l)[16], const float2 (&twv)[8]) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int k1 = 8 * q + i;
-      const float2 y = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
-      const float2 tv = cmul(y, twv[i]);
-      const __half2 hi = __floats2half2_rn(tv.x, tv.y);
-      const float2 hf = __half22float2(hi);
-      const __half2 lo = __floats2half2_rn(tv.x - hf.x, tv.y - hf.y);
-      const int mr = seq * S + k1;
-      const int off = (mr >> 3) * C::SBO + (r >> 2) * C::LBO + (mr & 7) * 16 + (r & 3) * 4;
-      *reinterpret_cast<__half2*>(sAhi + off) = hi;
-      *reinterpret_cast<__half2*>(sAlo + off) = lo;
-    }
-  };
   auto epi1 = [&]() {
-    if constexpr (NQ == 2) {
-      // both chunks' twiddles and accumulator columns requested before one wait
-      float2 twa[8], twb[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        twa[i] = sTw[(8 * half + i) * S + r];
-        twb[i] = sTw[(8 * (2 + half) + i) * S + r];
-      }
-      float h0[16], l0[16], h1[16], l1[16];
-      tc::tmem_ld16(d1 + lane_off + 16 * half, h0);
-      tc::tmem_ld16(d1 + lane_off + 2 * S + 16 * half, l0);
-      tc::tmem_ld16(d1 + lane_off + 16 * (2 + half), h1);
-      tc::tmem_ld16(d1 + lane_off + 2 * S + 16 * (2 + half), l1);
-      tc::tmem_wait_ld(h0, l0);
-      tc::tmem_wait_ld(h1, l1);
-      epi1_chunk(half, h0, l0, twa);
-      epi1_chunk(2 + half, h1, l1, twb);
-      return;
-    }
 #pragma unroll
     for (int qq = 0; qq < NQ; ++qq) {
       const int q = 2 * qq + half;
@@ -240,29 +205,23 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
       for (int i = 0; i < 8; ++i) twv[i] = sTw[(8 * q + i) * S + r];
       float h[16], l[16];
       tc::tmem_ld16x2(d1 + lane_off + 16 * q, d1 + lane_off + 2 * S + 16 * q, h, l);
-      epi1_chunk(q, h, l, twv);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int k1 = 8 * q + i;
+        const float2 y = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
+        const float2 tv = cmul(y, twv[i]);
+        const __half2 hi = __floats2half2_rn(tv.x, tv.y);
+        const float2 hf = __half22float2(hi);
+        const __half2 lo = __floats2half2_rn(tv.x - hf.x, tv.y - hf.y);
+        const int mr = seq * S + k1;
+        const int off = (mr >> 3) * C::SBO + (r >> 2) * C::LBO + (mr & 7) * 16 + (r & 3) * 4;
+        *reinterpret_cast<__half2*>(sAhi + off) = hi;
+        *reinterpret_cast<__half2*>(sAlo + off) = lo;
+      }
     }
   };
   // detection: lane seq S + k1 holds X[k1 + S k2] for all k2
   auto epi2 = [&](float (&acc)[NACC]) {
-    if constexpr (POL == POL_TP && NQ == 2) {
-      // both column chunks of the thread requested before one wait
-      float h0[16], l0[16], h1[16], l1[16];
-      tc::tmem_ld16(d2 + lane_off + 16 * half, h0);
-      tc::tmem_ld16(d2 + lane_off + 2 * S + 16 * half, l0);
-      tc::tmem_ld16(d2 + lane_off + 16 * (2 + half), h1);
-      tc::tmem_ld16(d2 + lane_off + 2 * S + 16 * (2 + half), l1);
-      tc::tmem_wait_ld(h0, l0);
-      tc::tmem_wait_ld(h1, l1);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float x0 = h0[2 * i] + l0[2 * i], y0 = h0[2 * i + 1] + l0[2 * i + 1];
-        const float x1 = h1[2 * i] + l1[2 * i], y1 = h1[2 * i + 1] + l1[2 * i + 1];
-        acc[i] = __fmaf_rn(y0, y0, __fmaf_rn(x0, x0, acc[i]));
-        acc[8 + i] = __fmaf_rn(y1, y1, __fmaf_rn(x1, x1, acc[8 + i]));
-      }
-      return;
-    }
 #pragma unroll
     for (int qq = 0; qq < NQ; ++qq) {
       const int q = 2 * qq + half;

@@ -106,10 +106,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mb, unsigned parity,
 }
 
 // ---- tensor memory -> registers ----
-// A load of 16 consecutive columns of this thread's lane (32x32b shape);
-// the values are valid only after tmem_wait_ld.
-__device__ __forceinline__ void tmem_ld16(uint32_t ta, float (&a)[16]) {
+// Two loads of 16 consecutive columns of this thread's lane (32x32b shape),
+// then the wait; the registers are tied to the wait so that no use of them
+// can be scheduled before it.
+__device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float (&a)[16], float (&b)[16]) {
   uint32_t* ra = reinterpret_cast<uint32_t*>(a);
+  uint32_t* rb = reinterpret_cast<uint32_t*>(b);
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
       "%15}, [%16];"
@@ -117,13 +119,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t ta, float (&a)[16]) {
         "=r"(ra[8]), "=r"(ra[9]), "=r"(ra[10]), "=r"(ra[11]), "=r"(ra[12]), "=r"(ra[13]), "=r"(ra[14]),
         "=r"(ra[15])
       : "r"(ta));
-}
-// Waits for this thread's tensor-memory loads; the registers of a and b are
-// tied to the wait so that no use of them can be scheduled before it (a
-// second wait for further registers returns at once).
-__device__ __forceinline__ void tmem_wait_ld(float (&a)[16], float (&b)[16]) {
-  uint32_t* ra = reinterpret_cast<uint32_t*>(a);
-  uint32_t* rb = reinterpret_cast<uint32_t*>(b);
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(rb[0]), "=r"(rb[1]), "=r"(rb[2]), "=r"(rb[3]), "=r"(rb[4]), "=r"(rb[5]), "=r"(rb[6]), "=r"(rb[7]),
+        "=r"(rb[8]), "=r"(rb[9]), "=r"(rb[10]), "=r"(rb[11]), "=r"(rb[12]), "=r"(rb[13]), "=r"(rb[14]),
+        "=r"(rb[15])
+      : "r"(tb));
   asm volatile(
       "tcgen05.wait::ld.sync.aligned;"
       : "+r"(ra[0]), "+r"(ra[1]), "+r"(ra[2]), "+r"(ra[3]), "+r"(ra[4]), "+r"(ra[5]), "+r"(ra[6]), "+r"(ra[7]),
@@ -133,12 +135,6 @@ __device__ __forceinline__ void tmem_wait_ld(float (&a)[16], float (&b)[16]) {
         "+r"(rb[14]), "+r"(rb[15])
       :
       : "memory");
-}
-// Two loads of 16 columns, then the wait.
-__device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float (&a)[16], float (&b)[16]) {
-  tmem_ld16(ta, a);
-  tmem_ld16(tb, b);
-  tmem_wait_ld(a, b);
 }
 
 }  // namespace tc
