@@ -79,6 +79,8 @@ typedef struct {
   size_t device_bytes;             /* device memory accounted to the job */
 } rawspec_gb300_job_stats;
 
+/* A job's statistics; those of finished jobs are kept until the server is
+ * destroyed.  0, or 1 for an unknown job. */
 int rawspec_gb300_server_job_stats(rawspec_gb300_server *s, int job, rawspec_gb300_job_stats *st);
 
 typedef struct {

@@ -394,11 +394,12 @@ void CUDART_CB post_dump_fn(void* data) {
 // ----------------------------------------------------------------------------
 // Memory.  Device buffers come from the device's stream-ordered memory pool
 // (cudaMallocAsync on the context stream, freed with cudaFreeAsync), which
-// keeps freed memory for later contexts and never synchronises the device, so
-// that creating and freeing contexts does not stall other contexts' work (a
-// job server runs many).  Page-locked host buffers (h_pwrbuf, h_icsbuf, the
-// library's host blocks) are likewise kept by size class for later contexts:
-// pinning memory costs milliseconds per allocation.
+// keeps up to 8 GiB of freed memory for later contexts (the rest returns to
+// the driver) and never synchronises the device, so that creating and freeing
+// contexts does not stall other contexts' work (a job server runs many).
+// Page-locked host buffers (h_pwrbuf, h_icsbuf, the library's host blocks)
+// are likewise kept by size class for later contexts, up to 8 GiB: pinning
+// memory costs milliseconds per allocation.
 // ----------------------------------------------------------------------------
 void keep_pool_memory(int device) {
   static std::mutex mu;
@@ -407,7 +408,7 @@ void keep_pool_memory(int device) {
   if (std::find(done.begin(), done.end(), device) != done.end()) return;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-    uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool (this process's memory only)
+    uint64_t keep = uint64_t(8) << 30;  // freed bytes the pool keeps (this process's memory only)
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   cudaGetLastError();
