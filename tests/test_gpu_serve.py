@@ -134,3 +134,28 @@ def test_job_larger_than_the_budget_is_rejected(cuda_device):
     with serve.Server(budget_bytes=1 << 20) as srv:
         with pytest.raises(ValueError):
             submit(srv, 0)
+
+
+def test_server_refuses_bad_requests(cuda_device):
+    import ctypes as Cc
+    with serve.Server(budget_bytes=1 << 30, max_active=2, max_queued=1) as srv:
+        job = submit(srv, 3)
+        nb, blocks = job_blocks(3)
+        with pytest.raises(RuntimeError):          # wrong buffer size
+            srv.push(job, blocks[:nb, :-16])
+        with pytest.raises(RuntimeError):          # unknown job
+            srv.push(job + 100, blocks[:nb])
+        assert srv.wait_job(job + 100, 0.1) == -1
+        with pytest.raises(KeyError):
+            srv.job_stats(job + 100)
+        srv.push(job, blocks[:nb])
+        srv.close_job(job)
+        with pytest.raises(RuntimeError):          # closed job
+            srv.push(job, blocks[:nb])
+        assert srv.wait_job(job, 60.0) == serve.JOB_DONE
+        st = srv.job_stats(job)
+        assert st.buffers == 1 and st.state == serve.JOB_DONE and st.device_bytes > 0
+        assert srv.stats().used == 0
+        # an invalid configuration is refused at submission
+        bad = api.make_context(16, 2, 1 << 15, 8, [(1000, 3, 1)])
+        assert serve.lib().rawspec_gb300_server_submit(srv.h, Cc.byref(bad), 1, srv._cb, None) == -1
