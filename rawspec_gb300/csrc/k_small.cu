@@ -55,7 +55,7 @@ __host__ __device__ constexpr size_t small_smem_bytes() {
   using C = SmallCfg<N, NP>;
   const size_t tw = (size_t)((C::TW + 1) & ~1) * sizeof(float2);
   const size_t xch = (C::T > 1) ? (size_t)C::G * NV * smem_padded_len(N) * sizeof(float2) : 0;
-  const size_t red = (size_t)C::TPB * C::R * NP * sizeof(float);
+  const size_t red = (size_t)C::G * (C::R * NP * C::T + 1) * sizeof(float);  // padded group slices
   return tw + (xch > red ? xch : red);
 }
 
@@ -189,12 +189,15 @@ k_small(SmallLaunch a) {
     }
   }
 
-  // Reduce across the groups of each set: red[g][p][m][j].
+  // Reduce across the groups of each set: red[g][p][m][j], each group's
+  // slice padded by one float so that the groups' writes fall into different
+  // banks (with one thread per transform they would all hit one bank).
+  constexpr int RS = NP * R * T + 1;
   __syncthreads();
 #pragma unroll
   for (int p = 0; p < NP; ++p)
 #pragma unroll
-    for (int m = 0; m < R; ++m) red[((g * NP + p) * R + m) * T + j] = acc[m][p];
+    for (int m = 0; m < R; ++m) red[g * RS + (p * R + m) * T + j] = acc[m][p];
   __syncthreads();
 
   const int set_threads = gps * T;
@@ -206,7 +209,7 @@ k_small(SmallLaunch a) {
     const int m = k / T;
     const int jj = k - m * T;
     float s = 0.0f;
-    for (int q = 0; q < gps; ++q) s += red[(((set * gps + q) * NP + p) * R + m) * T + jj];
+    for (int q = 0; q < gps; ++q) s += red[(set * gps + q) * RS + (p * R + m) * T + jj];
     if (a.chunks > 1) {
       a.partial[(((size_t)unit * a.chunks + chunk) * NP + p) * N + k] = s;
     } else {
