@@ -50,12 +50,22 @@ struct GroupSync {
   }
 };
 
+// Floats between the groups' slices of the reduction area: the slice
+// (NP R T floats) padded so that, with T < 32 threads per group, the groups
+// of a warp start T banks apart and their writes fall into distinct banks.
+template <int N, int NP>
+__host__ __device__ constexpr int small_red_stride() {
+  using C = SmallCfg<N, NP>;
+  constexpr int rb = NP * C::R * C::T;
+  return C::T >= 32 ? rb : rb + ((C::T - rb % 32) % 32 + 32) % 32;
+}
+
 template <int N, int NV, int NP>
 __host__ __device__ constexpr size_t small_smem_bytes() {
   using C = SmallCfg<N, NP>;
   const size_t tw = (size_t)((C::TW + 1) & ~1) * sizeof(float2);
   const size_t xch = (C::T > 1) ? (size_t)C::G * NV * smem_padded_len(N) * sizeof(float2) : 0;
-  const size_t red = (size_t)C::G * (C::R * NP * C::T + 1) * sizeof(float);  // padded group slices
+  const size_t red = (size_t)C::G * small_red_stride<N, NP>() * sizeof(float);
   return tw + (xch > red ? xch : red);
 }
 
@@ -189,10 +199,10 @@ k_small(SmallLaunch a) {
     }
   }
 
-  // Reduce across the groups of each set: red[g][p][m][j], each group's
-  // slice padded by one float so that the groups' writes fall into different
-  // banks (with one thread per transform they would all hit one bank).
-  constexpr int RS = NP * R * T + 1;
+  // Reduce across the groups of each set: red[g][p][m][j], the groups'
+  // slices padded apart (small_red_stride) so that their writes fall into
+  // different banks (with one thread per transform they would all hit one).
+  constexpr int RS = small_red_stride<N, NP>();
   __syncthreads();
 #pragma unroll
   for (int p = 0; p < NP; ++p)
