@@ -177,20 +177,16 @@ __device__ __forceinline__ unsigned long long policy_evict_last() {
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
   return p;
 }
-// The ring and output stores carry no memory clobber: no thread reads what
-// it stores here with ordinary loads (the ring is read back through bulk
-// copies after the CTA barrier and fence of publish()), and without the
-// clobber the compiler may hoist the next twiddle's shared-memory load above
-// a store instead of waiting for each in turn.
 __device__ __forceinline__ void st_f2_hint(float2* p, float2 v, unsigned long long pol) {
-  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol));
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
 }
 __device__ __forceinline__ void st_f_hint(float* p, float v, unsigned long long pol) {
-  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol));
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
 }
 // *p += v, performed in L2 without returning a value (no wait on the thread).
 __device__ __forceinline__ void red_add_f_hint(float* p, float v, unsigned long long pol) {
-  asm volatile("red.global.add.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol));
+  asm volatile("red.global.add.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
 }
 
 // ---- mbarrier and bulk-copy primitives (PTX ISA: mbarrier, cp.async.bulk) ----
