@@ -391,6 +391,10 @@ def run_native(args, rank, world, local_rank):
 
     from rawspec_gb300 import api, synth
 
+    # the CPU baseline first, on an otherwise idle host (after the GPU legs it
+    # measured up to 40 % lower in the same process)
+    cpu = cpu_baseline_leg() if rank == 0 and world == 1 and not args.no_cpu else None
+
     torch.cuda.set_device(local_rank)
     group = RankGroup(world)
     barrier, max_over_ranks = group.barrier, group.max_over_ranks
@@ -558,7 +562,7 @@ def run_native(args, rank, world, local_rank):
         "device_bytes": r["device_bytes"],
     }
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline_leg()
+        line["cpu_baseline"] = cpu
     if rank == 0 and world == 1 and not args.no_ingest:
         line["ingest"] = ingest_leg()
     if rank == 0 and world == 1 and not args.no_serve:
