@@ -46,16 +46,29 @@ struct BlockSyncL {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
+// float2 between the exchange areas of neighbouring sub-FFTs (NV buffers of
+// smem_padded_len(N) each): at least their size, and chosen so that the C
+// sub-FFTs served by one half-warp start in different banks (their start
+// offsets modulo 16 float2 are multiples of 16 / C), even for 16-byte rows.
+template <int N, int C, int NV>
+__host__ __device__ constexpr int sub_stride() {
+  int base = NV * smem_padded_len(N);
+  const int cp = C < 16 ? C : 16;
+  const int want = (16 / cp) % 16;
+  while (base % 16 != want) ++base;
+  return base + (base & 1);
+}
+
 template <int N2, int NV>
 constexpr size_t passA_smem() {
   using Cf = LargeCfg<N2, kRA>;
-  return (size_t)((Cf::TW + 1) & ~1) * sizeof(float2) + (size_t)Cf::C * NV * smem_padded_len(N2) * sizeof(float2);
+  return (size_t)((Cf::TW + 1) & ~1) * sizeof(float2) + (size_t)Cf::C * sub_stride<N2, Cf::C, NV>() * sizeof(float2);
 }
 
 template <int N1, int NV, int R>
 constexpr size_t passB_smem() {
   using Cf = LargeCfg<N1, R>;
-  return (size_t)((Cf::TW + 1) & ~1) * sizeof(float2) + (size_t)Cf::C * NV * smem_padded_len(N1) * sizeof(float2);
+  return (size_t)((Cf::TW + 1) & ~1) * sizeof(float2) + (size_t)Cf::C * sub_stride<N1, Cf::C, NV>() * sizeof(float2);
 }
 
 }  // namespace
@@ -102,7 +115,7 @@ k_large_a(LargeLaunch a) {
   const int e0 = n1 * j;
   const float2 w0 = cmul(__ldg(a.twLo + (e0 & ((1 << a.h) - 1))), __ldg(a.twHi + (e0 >> a.h)));
   __syncthreads();  // twiddle table in shared memory
-  GroupFFT<N2, R, NV>::run(v, j, xch + (size_t)col * NV * smem_padded_len(N2), smem_padded_len(N2), tw_s,
+  GroupFFT<N2, R, NV>::run(v, j, xch + (size_t)col * sub_stride<N2, C, NV>(), smem_padded_len(N2), tw_s,
                             BlockSyncL{});
 
   // Output k2 = j + m*T: W_N^(n1*k2) = W_N^(n1*j) * W_N^(n1*m*T).
@@ -154,7 +167,7 @@ k_large_b(LargeLaunch a) {
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[m][p] = 0.0f;
 
-  float2* my_xch = xch + (size_t)row * NV * smem_padded_len(N1);
+  float2* my_xch = xch + (size_t)row * sub_stride<N1, C, NV>();
   for (int sl = s_begin; sl < s_end; ++sl) {
     const int slab = c * a.Nss + d * a.M + sl;
     const float2* src = a.scratch + ((size_t)slab * NV * N2 + k2) * N1 + j;
