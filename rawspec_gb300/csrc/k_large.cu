@@ -26,7 +26,11 @@ namespace {
 
 constexpr int kRA = 16;  // radix of pass A
 constexpr int kLargeTPB = 256;
-constexpr int kLargeMinBlocks = 2;  // resident CTAs per SM the register budget allows
+// Resident CTAs per SM the register budget allows: one polarisation fits
+// 80 registers a thread without spills (three CTAs of 256 threads), two
+// polarisations need about 128 (two CTAs).
+template <int NV>
+constexpr int large_min_blocks() { return NV == 1 ? 3 : 2; }
 
 // Sub-FFT of NSUB points at radix R; C sub-FFTs (columns or rows) per CTA,
 // interleaved across lanes so that global accesses of neighbouring lanes are
@@ -74,7 +78,7 @@ constexpr size_t passB_smem() {
 }  // namespace
 
 template <int N2, int FMT, int NV>
-__global__ void __launch_bounds__(LargeCfg<N2, kRA>::TPB, kLargeMinBlocks)
+__global__ void __launch_bounds__(LargeCfg<N2, kRA>::TPB, large_min_blocks<NV>())
 k_large_a(LargeLaunch a) {
   using Cf = LargeCfg<N2, kRA>;
   constexpr int R = kRA, T = Cf::T, C = Cf::C, TPB = Cf::TPB;
@@ -131,7 +135,7 @@ k_large_a(LargeLaunch a) {
 }
 
 template <int N1, int NV, int POL>
-__global__ void __launch_bounds__(LargeCfg<N1, pass_b_radix<POL>()>::TPB, kLargeMinBlocks)
+__global__ void __launch_bounds__(LargeCfg<N1, pass_b_radix<POL>()>::TPB, large_min_blocks<NV>())
 k_large_b(LargeLaunch a) {
   constexpr int R = pass_b_radix<POL>();
   using Cf = LargeCfg<N1, R>;

@@ -2,12 +2,14 @@
 profiling a single kernel with Nsight Compute.
 
 usage: python -m rawspec_gb300.profile_case --nc 64 --ntpb 524288 --nt 1048576 --na 51 [--npol 1] [--buffers 2]
-       [--nbits 4|8|16] [--np 1|2] [--nant A --ics] [--copy-each]
+       [--nbits 4|8|16] [--np 1|2] [--nant A --ics] [--copy-each] [--timing]
 
 Input: seeded Gaussian voltages (sigma 20; 4-bit: uniform with per-antenna
 gains), device resident after the first copy (or copied, and expanded, for
 every buffer with --copy-each); each buffer is processed with
-rawspec_start_processing.
+rawspec_start_processing.  --timing then processes 3 more buffers and times
+10 with the library's per-kernel-class CUDA events, printing the average
+microseconds per buffer of each class.
 """
 from __future__ import annotations
 
@@ -32,6 +34,7 @@ def main() -> int:
     ap.add_argument("--nb", type=int, default=0)
     ap.add_argument("--buffers", type=int, default=2)
     ap.add_argument("--copy-each", action="store_true", help="copy (and expand 4-bit) the blocks for every buffer")
+    ap.add_argument("--timing", action="store_true", help="time 10 more buffers per kernel class")
     a = ap.parse_args()
     from rawspec_gb300 import api, synth
     prods = [(nt, na, a.npol) for nt, na in zip(a.nt, a.na)]
@@ -50,6 +53,23 @@ def main() -> int:
             spec.start()
         rc = spec.wait()
         print(f"processed {a.buffers} buffers of {spec.Nb} blocks, launches {spec.kernel_launches()}, rc {rc}")
+        if a.timing and rc == 0:
+            for _ in range(3):
+                spec.start()
+            spec.wait()
+            spec.reset_profile()
+            spec.set_profiling(True)
+            for _ in range(10):
+                if a.copy_each:
+                    spec.copy_to_gpu()
+                spec.start()
+            rc = spec.wait()
+            us = {}
+            for k, name in enumerate(api.KERNEL_CLASS_NAMES):
+                ms, n = spec.profile(k)[:2]
+                if n:
+                    us[name] = round(ms * 1e3 / 10, 1)
+            print(f"microseconds per buffer by kernel class: {us}")
     return rc
 
 
