@@ -25,7 +25,8 @@ enum rawspec_gb300_kernel_class {
   RAWSPEC_GB300_K_H2D = 7,      /* block copies host -> device                */
   RAWSPEC_GB300_K_LARGE_FUSED = 8, /* persistent fused four-step kernel       */
   RAWSPEC_GB300_K_TC = 9,       /* tensor-core DFT product kernel             */
-  RAWSPEC_GB300_K_COUNT = 10
+  RAWSPEC_GB300_K_MERGE = 10,   /* compensated integration across buffers     */
+  RAWSPEC_GB300_K_COUNT = 11
 };
 
 /* Validates and normalises a context exactly as rawspec_initialize() does

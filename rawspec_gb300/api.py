@@ -28,7 +28,8 @@ RAWSPEC_CALLBACK_PRE_DUMP = 0
 RAWSPEC_CALLBACK_POST_DUMP = 1
 
 K_SMALL, K_FINALIZE, K_LARGE_A, K_LARGE_B, K_ICS, K_EXPAND4, K_D2H, K_H2D, K_LARGE_FUSED = range(9)
-KERNEL_CLASS_NAMES = ["small", "finalize", "large_a", "large_b", "ics", "expand4", "d2h", "h2d", "large_fused", "tc"]
+KERNEL_CLASS_NAMES = ["small", "finalize", "large_a", "large_b", "ics", "expand4", "d2h", "h2d", "large_fused", "tc",
+                      "merge"]
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "librawspec.so"
 

@@ -204,4 +204,10 @@ struct IcsLaunch {
 };
 cudaError_t ics_launch(const IcsLaunch& L, cudaStream_t s);
 
+// Compensated (Kahan) integration across buffers, elementwise over n floats:
+// y = stage - comp; t = sum + y; comp = (t - sum) - y; sum = t.  Products
+// whose integration spans many buffers write each later buffer into `stage`
+// and fold it into the running sum with this step.
+cudaError_t kahan_merge_launch(float* sum, float* comp, const float* stage, long long n, cudaStream_t s);
+
 }  // namespace rsg

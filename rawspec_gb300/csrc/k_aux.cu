@@ -1,6 +1,7 @@
-// k_aux.cu -- plan-time twiddle tables, 4-bit expansion and the weighted
-// incoherent sum across antennas.
+// k_aux.cu -- plan-time twiddle tables, 4-bit expansion, the weighted
+// incoherent sum across antennas and the compensated integration step.
 #include <algorithm>
+#include <cstdint>
 
 #include "common.cuh"
 #include "internal.h"
@@ -197,6 +198,56 @@ cudaError_t ics_launch(const IcsLaunch& L, cudaStream_t s) {
   const long long total = (long long)L.Nd * L.np * (L.Nc / L.Nant) * L.N;
   const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 152LL * 16));
   k_ics<<<blocks, 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+// One step of compensated summation (Kahan, "Further remarks on reducing
+// truncation errors", CACM 8(1), 1965): the low-order part lost when x is
+// added to s is carried in c and taken off the next term.  Round-to-nearest
+// intrinsics keep the compiler from contracting or reassociating the four
+// operations.
+__device__ __forceinline__ void kahan_step(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+// Streams the three planes once: 16-byte accesses over the first n4 groups
+// of four floats, single floats over the tail.
+__global__ void k_kahan_merge(float* __restrict__ sum, float* __restrict__ comp, const float* __restrict__ stage,
+                              long long n, long long n4) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float4* s4 = reinterpret_cast<float4*>(sum);
+  float4* c4 = reinterpret_cast<float4*>(comp);
+  const float4* x4 = reinterpret_cast<const float4*>(stage);
+  for (long long i = i0; i < n4; i += stride) {
+    float4 s = s4[i], c = c4[i];
+    const float4 x = __ldcs(x4 + i);
+    kahan_step(s.x, c.x, x.x);
+    kahan_step(s.y, c.y, x.y);
+    kahan_step(s.z, c.z, x.z);
+    kahan_step(s.w, c.w, x.w);
+    s4[i] = s;
+    c4[i] = c;
+  }
+  for (long long i = 4 * n4 + i0; i < n; i += stride) {
+    float s = sum[i], c = comp[i];
+    kahan_step(s, c, __ldcs(stage + i));
+    sum[i] = s;
+    comp[i] = c;
+  }
+}
+
+cudaError_t kahan_merge_launch(float* sum, float* comp, const float* stage, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const bool vec = ((reinterpret_cast<uintptr_t>(sum) | reinterpret_cast<uintptr_t>(comp) |
+                     reinterpret_cast<uintptr_t>(stage)) & 15) == 0;
+  const long long n4 = vec ? n / 4 : 0;
+  const long long items = std::max(n4, n - 4 * n4);
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((items + 255) / 256, 152LL * 8));
+  k_kahan_merge<<<blocks, 256, 0, s>>>(sum, comp, stage, n, n4);
   return cudaGetLastError();
 }
 

@@ -75,6 +75,10 @@ struct Product {
   int* d_ctl = nullptr;    // control words of the fused kernel (error word first) or the tc error word
   int* h_err = nullptr;    // pinned copy of the error word, refreshed after every fused or tc launch
   float* d_partial = nullptr;  // per-chunk partial sums of this product
+  bool kahan = false;          // compensated integration across buffers
+  float* d_stage = nullptr;    // this buffer's sums (out_bytes), folded into d_out by k_kahan_merge
+  float* d_comp = nullptr;     // running compensation of d_out (out_bytes)
+  CUtensorMap tmap_stage;      // the fused kernel's output map of d_stage
   float2* d_scratch = nullptr; // four-step intermediate (or the fused kernel's ring)
   cudaStream_t own_stream = nullptr;  // the product's kernels run concurrently with the others'
   cudaStream_t stream = nullptr;      // stream of the current buffer (own_stream, or the context
@@ -215,6 +219,23 @@ bool tensor_dft_wanted(int logN, int pol) {
   if (v && v[0] == '0') return false;
   if (v && v[0] == '1') return true;
   return (logN == 10 || logN == 12) && pol == POL_TP;
+}
+
+// Products whose integration spans buffers (Nis > 1) and runs over at least
+// 3072 spectra integrate across buffers with compensated (Kahan) summation:
+// the first buffer of an integration writes the sum, every later one writes
+// a staging plane that k_kahan_merge folds into the sum and its compensation
+// plane.  Within a buffer the sums are already blocked (per-thread runs,
+// chunk partials in fixed order), so the one long sequential chain is the
+// chain across buffers.  RAWSPEC_GB300_KAHAN=1 / =0 at initialisation
+// selects compensation for every product with Nis > 1 / for none.
+constexpr unsigned kKahanMinNint = 3072;
+bool kahan_wanted(unsigned Na, unsigned Nis) {
+  if (Nis <= 1) return false;
+  const char* v = getenv("RAWSPEC_GB300_KAHAN");
+  if (v && v[0] == '0') return false;
+  if (v && v[0] == '1') return true;
+  return Na >= kKahanMinNint;
 }
 
 int validate_impl(rawspec_context* ctx, bool* expanded) {
@@ -478,11 +499,11 @@ int dev_alloc(GpuCtx* g, T** p, size_t bytes) {
   return 0;
 }
 
-int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int unit0, int n_units, int chunks, int upc,
-                    int mode, int inverse, float scale) {
+int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, float* out, int unit0, int n_units, int chunks,
+                    int upc, int mode, int inverse, float scale) {
   FinalizeLaunch F;
   F.partial = P.d_partial;
-  F.out = P.d_out;
+  F.out = out;
   F.unit0 = unit0;
   F.n_units = n_units;
   F.chunks = chunks;
@@ -499,11 +520,17 @@ int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, int unit0
   return 0;
 }
 
-// Queues product i's kernels for the channels [c0, c1) of the buffer.
+// Queues product i's kernels for the channels [c0, c1) of the buffer.  With
+// compensated integration the buffers after an integration's first write
+// their sums to the staging plane.
 int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse, int c0, int c1) {
   Product& P = g->prod[i];
+  const bool staged = P.kahan && mode == ACC_ADD;
+  float* const out = staged ? P.d_stage : P.d_out;
+  if (staged) mode = ACC_WRITE;
   if (P.tc) {
     TcLaunch L = P.tl;
+    L.out = out;
     L.mode = mode;
     L.inverse = inverse;
     L.unit0 = c0 * L.units_per_chan;
@@ -518,13 +545,14 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
       g->launches++;
     }
     if (L.chunks > 1 &&
-        launch_finalize(ctx, g, P, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+        launch_finalize(ctx, g, P, out, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
       return 1;
     RSG_CUDA(cudaMemcpyAsync(P.h_err, P.d_ctl, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
     return 0;
   }
   if (!P.large) {
     SmallLaunch L = P.sl;
+    L.out = out;
     L.mode = mode;
     L.inverse = inverse;
     L.unit0 = c0 * L.units_per_chan;
@@ -539,10 +567,12 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
       g->launches++;
     }
     if (L.chunks > 1 &&
-        launch_finalize(ctx, g, P, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+        launch_finalize(ctx, g, P, out, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
       return 1;
   } else {
     LargeLaunch L = P.ll;
+    L.out = out;
+    if (staged) L.tmap_out = P.tmap_stage;
     L.mode = mode;
     L.inverse = inverse;
     L.slab0 = c0 * L.Nss;
@@ -572,7 +602,7 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
       g->launches++;
     }
     if (L.chunks > 1 &&
-        launch_finalize(ctx, g, P, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
+        launch_finalize(ctx, g, P, out, L.unit0, L.unit_count, L.chunks, L.units_per_chan, mode, inverse, L.scale))
       return 1;
   }
   return 0;
@@ -605,6 +635,16 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
   }
   for (unsigned i = 0; i < ctx->No; i++) {
     Product& P = g->prod[i];
+    if (P.kahan) {
+      const long long n = (long long)(P.out_bytes / sizeof(float));
+      if (mode[i] == ACC_WRITE) {
+        RSG_CUDA(cudaMemsetAsync(P.d_comp, 0, P.out_bytes, P.stream));
+      } else {
+        ProfScope ps(g, RAWSPEC_GB300_K_MERGE, P.stream);
+        RSG_CUDA(kahan_merge_launch(P.d_out, P.d_comp, P.d_stage, n, P.stream));
+        g->launches++;
+      }
+    }
     if (g->inbuf_count % P.Nis == 0) {
       if (ctx->incoherently_sum) {
         IcsLaunch I;
@@ -661,6 +701,7 @@ int plan_device_bytes(const rawspec_context* ctx, bool expanded, int sm_count, s
     const int M = (int)(Nis > 1 ? Nss : ctx->Nas[i]);
     const int upc = (int)(Nis > 1 ? 1 : Nss / ctx->Nas[i]);
     t += ctx->h_pwrbuf_size[i];
+    if (kahan_wanted(ctx->Nas[i], Nis)) t += 2 * ctx->h_pwrbuf_size[i];
     if (ctx->incoherently_sum) t += ctx->h_pwrbuf_size[i] / ctx->Nant;
     const bool large = logN > 12;
     if (!large && tensor_dft_wanted(logN, pol) && tc_supported(logN, fmt, (int)ctx->Np, pol, M)) {
@@ -874,6 +915,12 @@ int rawspec_initialize(rawspec_context* ctx) {
     P.out_bytes = ctx->h_pwrbuf_size[i];
     if (dev_alloc(g, &P.d_out, P.out_bytes)) FAIL();
     CK(cudaMemsetAsync(P.d_out, 0, P.out_bytes, g->stream));
+    P.kahan = kahan_wanted(P.Na, P.Nis);
+    if (P.kahan) {
+      if (dev_alloc(g, &P.d_stage, P.out_bytes)) FAIL();
+      if (dev_alloc(g, &P.d_comp, P.out_bytes)) FAIL();
+      CK(cudaMemsetAsync(P.d_comp, 0, P.out_bytes, g->stream));
+    }
     if (ctx->incoherently_sum) {
       P.ics_bytes = ctx->h_pwrbuf_size[i] / ctx->Nant;
       CK(pinned_alloc((void**)&ctx->h_icsbuf[i], P.ics_bytes));
@@ -999,8 +1046,17 @@ int rawspec_initialize(rawspec_context* ctx) {
       CK(twiddle_fill(P.d_tw + o_hi, (long long)nhi, (long long)P.N, (long long)nlo, g->stream));
       CK(passa_twiddle_fill(P.d_tw + o_m, n1, RA, (long long)(n2 / RA), (long long)P.N, g->stream));
       if (P.fused) CK(passa_twiddle_fill(P.d_tw + o_j, n1, n2 / RA, 1, (long long)P.N, g->stream));
-      if (P.fused) CK(large_fused_prepare(L));
-      else CK(large_prepare(L));
+      if (P.fused) {
+        if (P.kahan) {  // the same maps over the staging plane; its output map is kept
+          LargeLaunch Ls = L;
+          Ls.out = P.d_stage;
+          CK(large_fused_prepare(Ls));
+          P.tmap_stage = Ls.tmap_out;
+        }
+        CK(large_fused_prepare(L));
+      } else {
+        CK(large_prepare(L));
+      }
     }
   }
   for (unsigned i = 0; i < ctx->No; i++) {
@@ -1060,6 +1116,8 @@ void rawspec_cleanup(rawspec_context* ctx) {
     pinned_free(g->prod[i].h_err, sizeof(int));
     dfree(g->prod[i].d_partial);
     dfree(g->prod[i].d_scratch);
+    dfree(g->prod[i].d_stage);
+    dfree(g->prod[i].d_comp);
     if (g->prod[i].own_stream) cudaStreamDestroy(g->prod[i].own_stream);
     if (g->prod[i].ev_join) cudaEventDestroy(g->prod[i].ev_join);
   }

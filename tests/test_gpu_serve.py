@@ -58,7 +58,9 @@ def test_device_bytes_estimate_equals_the_allocation(cuda_device):
     cases = [(64, 2, 1 << 19, 8, [(1 << 20, 51, 1), (8, 128, 1), (1024, 3072, 1)], 1, None),
              (64, 2, 1 << 19, 8, [(1 << 20, 51, 4), (8, 128, 4), (1024, 3072, 4)], 1, None),
              (16, 2, 1 << 18, 4, [(4096, 64, -4), (64, 1024, -4)], 4, [1.0, 0.5, 1.5, 1.0]),
-             (4, 1, 1 << 16, 16, [(1 << 17, 1, 1), (512, 8, 1)], 1, None)]
+             (4, 1, 1 << 16, 16, [(1 << 17, 1, 1), (512, 8, 1)], 1, None),
+             # integrations of >= 3072 spectra over many buffers: staging and compensation planes
+             (2, 2, 1 << 16, 8, [(1 << 16, 4096, 1), (256, 3072, 4)], 1, None)]
     for Nc, Np, Ntpb, nbits, prods, Nant, w in cases:
         ctx = api.make_context(Nc, Np, Ntpb, nbits, prods, Nant=Nant, weights=w)
         est = serve.device_bytes_estimate(ctx)
