@@ -68,6 +68,30 @@ unsigned long long rawspec_gb300_kernel_launches(rawspec_context *ctx);
 /* Bytes of device memory held by the context. */
 size_t rawspec_gb300_device_bytes(rawspec_context *ctx);
 
+/* Kernel class that computes product `product` of an initialised context:
+ * RAWSPEC_GB300_K_SMALL, RAWSPEC_GB300_K_TC, RAWSPEC_GB300_K_LARGE_FUSED or
+ * RAWSPEC_GB300_K_LARGE_A (the two-kernel four-step path); -1 if the
+ * context is not initialised or has no such product. */
+int rawspec_gb300_product_kernel(rawspec_context *ctx, int product);
+
+/* Kernel choices of one entry of the tuning table (RAWSPEC_GB300_TUNE_FILE,
+ * format in rawspec_gb300/csrc/tune.c); -1 (dft) or 0 (the others) leaves
+ * the library's own choice. */
+typedef struct {
+  int dft;   /* N <= 4096: 1 tensor-core DFT (k_tc, where supported), 0 CUDA cores (k_small) */
+  int ctas;  /* CTAs per SM that the chunking of k_small / k_large_a/b aims for (default 4) */
+  int lag;   /* k_large_fused: the row tiles of slab s follow the column tiles of slab s + lag */
+  int ring;  /* k_large_fused: intermediate slabs (> lag) */
+} rawspec_gb300_tune;
+
+/* Looks (nfft, nbits, npolout) up in the tuning table named by
+ * RAWSPEC_GB300_TUNE_FILE, read at each call; nbits is the width of the
+ * samples the kernels read (4-bit input is expanded to 8).  Returns 1 and
+ * fills *t if the table has the entry, 0 if it has not or no table is named
+ * (*t then holds the unset values), -1 if the file cannot be read.  Used
+ * by rawspec_initialize and the device-memory estimate; no CUDA calls. */
+int rawspec_gb300_tune_lookup(unsigned nfft, int nbits, int npolout, rawspec_gb300_tune *t);
+
 /* Device memory rawspec_initialize() would allocate for this context (the
  * same validation and kernel configuration, nothing allocated; the context
  * itself is not modified).  Needs the CUDA device gpu_index.  0 on success,

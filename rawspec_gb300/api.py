@@ -34,6 +34,18 @@ KERNEL_CLASS_NAMES = ["small", "finalize", "large_a", "large_b", "ics", "expand4
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "librawspec.so"
 
 
+class TuneEntry(C.Structure):
+    """rawspec_gb300_tune: one entry of the tuning table (-1 / 0: unset)."""
+    _fields_ = [("dft", C.c_int), ("ctas", C.c_int), ("lag", C.c_int), ("ring", C.c_int)]
+
+
+def tune_lookup(nfft: int, nbits: int, npolout: int) -> tuple[int, TuneEntry]:
+    """rawspec_gb300_tune_lookup: (1 found / 0 not / -1 unreadable, entry)."""
+    t = TuneEntry()
+    r = load_library().rawspec_gb300_tune_lookup(nfft, nbits, npolout, C.byref(t))
+    return int(r), t
+
+
 class RawspecContext(C.Structure):
     pass
 
@@ -108,6 +120,8 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
             "rawspec_gb300_reset_profile": (C.c_int, [P]),
             "rawspec_gb300_kernel_launches": (C.c_ulonglong, [P]),
             "rawspec_gb300_device_bytes": (C.c_size_t, [P]),
+            "rawspec_gb300_product_kernel": (C.c_int, [P, C.c_int]),
+            "rawspec_gb300_tune_lookup": (C.c_int, [C.c_uint, C.c_int, C.c_int, C.POINTER(TuneEntry)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -267,6 +281,14 @@ class Spectrometer:
 
     def reset_profile(self) -> None:
         self.lib.rawspec_gb300_reset_profile(C.byref(self.ctx))
+
+    def product_kernel(self, i: int) -> str:
+        """Name of the kernel class that computes product i ("small", "tc",
+        "large_fused" or "large_a" for the two-kernel path)."""
+        k = int(self.lib.rawspec_gb300_product_kernel(C.byref(self.ctx), i))
+        if k < 0:
+            raise ValueError(f"no product {i}")
+        return KERNEL_CLASS_NAMES[k]
 
     def kernel_launches(self) -> int:
         return int(self.lib.rawspec_gb300_kernel_launches(C.byref(self.ctx)))

@@ -213,12 +213,40 @@ bool graphs_wanted(const GpuCtx* g) {
 // k_small (k_tc is as fast alone but slows a mixed step with the fused
 // kernel), N = 256 too (k_tc is slower).  RAWSPEC_GB300_TENSOR_DFT=1 at
 // initialisation selects k_tc for every case it supports (N = 256, 1024,
-// 4096, all modes up to 1024), =0 for none.
-bool tensor_dft_wanted(int logN, int pol) {
+// 4096, all modes up to 1024), =0 for none.  Without the variable, a
+// tuning-table entry's dft= decides before the default.
+bool tensor_dft_wanted(int logN, int pol, const rawspec_gb300_tune& t) {
   const char* v = getenv("RAWSPEC_GB300_TENSOR_DFT");
   if (v && v[0] == '0') return false;
   if (v && v[0] == '1') return true;
+  if (t.dft >= 0) return t.dft == 1;
   return (logN == 10 || logN == 12) && pol == POL_TP;
+}
+
+// Tuning-table entry of product i of a validated context (unset values if
+// the table has none).
+rawspec_gb300_tune tune_for(const rawspec_context* ctx, int i) {
+  rawspec_gb300_tune t;
+  rawspec_gb300_tune_lookup(ctx->Nts[i], ctx->Nbps == 16 ? 16 : 8, ctx->Npolout[i], &t);
+  return t;
+}
+
+// CTAs per SM the chunking of k_small and k_large_a/b aims for.
+constexpr int kDefaultCtasPerSm = 4;
+int target_ctas_for(int sm_count, const rawspec_gb300_tune& t) {
+  return sm_count * (t.ctas > 0 ? t.ctas : kDefaultCtasPerSm);
+}
+
+// A tuning-table lag / ring of the fused kernel replaces the plan's; the
+// ring stays longer than the lag, the lag of channel-group launches no
+// longer than the ring allows.
+void apply_fused_tune(LargeLaunch& L, const rawspec_gb300_tune& t) {
+  const bool pipe_env = getenv("RAWSPEC_GB300_FUSED_LAG_PIPE") != nullptr;
+  if (t.lag > 0) L.lag = t.lag;
+  if (t.ring > 0) L.ring = t.ring;
+  if (L.ring <= L.lag) L.ring = L.lag + 2;
+  if (t.lag > 0 && !pipe_env) L.lag_pipe = L.lag;
+  L.lag_pipe = std::max(1, std::min(L.lag_pipe, L.ring - 1));
 }
 
 // Products whose integration spans buffers (Nis > 1) and runs over at least
@@ -690,7 +718,6 @@ int plan_device_bytes(const rawspec_context* ctx, bool expanded, int sm_count, s
   t += in_bytes;
   if (expanded) t += in_bytes / 2;
   if (ctx->incoherently_sum) t += ctx->Nant * sizeof(float);
-  const int target_ctas = sm_count * 4;
   const int groups = std::min<int>(kMaxCopyGroups, (int)ctx->Nc);
   auto al = [](size_t n) { return (n + 31) & ~size_t(31); };
   for (unsigned i = 0; i < ctx->No; i++) {
@@ -700,11 +727,13 @@ int plan_device_bytes(const rawspec_context* ctx, bool expanded, int sm_count, s
     const int pol = np == 1 ? POL_TP : ctx->Npolout[i];
     const int M = (int)(Nis > 1 ? Nss : ctx->Nas[i]);
     const int upc = (int)(Nis > 1 ? 1 : Nss / ctx->Nas[i]);
+    const rawspec_gb300_tune tune = tune_for(ctx, (int)i);
+    const int target_ctas = target_ctas_for(sm_count, tune);
     t += ctx->h_pwrbuf_size[i];
     if (kahan_wanted(ctx->Nas[i], Nis)) t += 2 * ctx->h_pwrbuf_size[i];
     if (ctx->incoherently_sum) t += ctx->h_pwrbuf_size[i] / ctx->Nant;
     const bool large = logN > 12;
-    if (!large && tensor_dft_wanted(logN, pol) && tc_supported(logN, fmt, (int)ctx->Np, pol, M)) {
+    if (!large && tensor_dft_wanted(logN, pol, tune) && tc_supported(logN, fmt, (int)ctx->Np, pol, M)) {
       TcLaunch L;
       L.logN = logN;
       L.pol = pol;
@@ -747,6 +776,7 @@ int plan_device_bytes(const rawspec_context* ctx, bool expanded, int sm_count, s
       if (fused) {
         L.S = (int)ctx->Nc * (int)Nss;
         if (large_fused_plan(L) != cudaSuccess) return 1;
+        apply_fused_tune(L, tune);
         sf = (size_t)std::min(L.ring, L.S) * L.nv * ((size_t)1 << L.logN);
         pf = 0;
         t += (size_t)large_fused_ctl_ints(L) * sizeof(int);
@@ -775,6 +805,15 @@ extern "C" {
 const char* get_librawspec_version() { return RSG_STR(RAWSPEC_GB300_VERSION) "-gb300"; }
 
 const char* get_cufft_version() { return "none (native sm_103a FFT)"; }
+
+int rawspec_gb300_product_kernel(rawspec_context* ctx, int product) {
+  GpuCtx* g = G(ctx);
+  if (!g || product < 0 || product >= (int)ctx->No) return -1;
+  const Product& P = g->prod[product];
+  if (P.tc) return RAWSPEC_GB300_K_TC;
+  if (!P.large) return RAWSPEC_GB300_K_SMALL;
+  return P.fused ? RAWSPEC_GB300_K_LARGE_FUSED : RAWSPEC_GB300_K_LARGE_A;
+}
 
 int rawspec_gb300_validate(rawspec_context* ctx) {
   bool expanded = false;
@@ -899,9 +938,10 @@ int rawspec_initialize(rawspec_context* ctx) {
   // (1/127 or 1/32767 per component) is applied to the quadratic products.
   const float snorm_d = ctx->Nbps == 16 ? 32767.0f : 127.0f;
   const float scale = 1.0f / (snorm_d * snorm_d);
-  const int target_ctas = g->sm_count * 4;
   for (unsigned i = 0; i < ctx->No; i++) {
     Product& P = g->prod[i];
+    const rawspec_gb300_tune tune = tune_for(ctx, (int)i);
+    const int target_ctas = target_ctas_for(g->sm_count, tune);
     P.N = (int)ctx->Nts[i];
     P.logN = ilog2u(ctx->Nts[i]);
     P.np = abs(ctx->Npolout[i]);
@@ -929,7 +969,7 @@ int rawspec_initialize(rawspec_context* ctx) {
     }
 
     P.large = P.logN > 12;
-    P.tc = !P.large && tensor_dft_wanted(P.logN, pol) && tc_supported(P.logN, g->fmt, (int)ctx->Np, pol, M);
+    P.tc = !P.large && tensor_dft_wanted(P.logN, pol, tune) && tc_supported(P.logN, g->fmt, (int)ctx->Np, pol, M);
     if (P.tc) {
       TcLaunch& L = P.tl;
       L.logN = P.logN;
@@ -1009,6 +1049,7 @@ int rawspec_initialize(rawspec_context* ctx) {
         P.fused = true;
         L.S = (int)ctx->Nc * (int)P.Nss;
         CK(large_fused_plan(L));
+        apply_fused_tune(L, tune);
         // slots in use: slab mod ring over at most S slabs
         sf = (size_t)std::min(L.ring, L.S) * L.nv * ((size_t)1 << L.logN);
         pf = 0;
