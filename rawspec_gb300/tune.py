@@ -1,14 +1,19 @@
 """Autotuner of the kernel choices per (FFT length, sample bits, Npolout).
 
 usage: python -m rawspec_gb300.tune --nc 64 --ntpb 524288 --nt 1048576 --na 51 --nt 8 --na 128 --nt 1024 --na 3072
-       [--np 2] [--nbits 8] [--npol 1] [--steps 20] [--reps 3] [--passes 1] [--out tuning.txt]
+       [--np 2] [--nbits 8] [--npol 1] [--steps 20] [--reps 3] [--rounds 2] [--passes 1] [--min-gain 0.02]
+       [--out tuning.txt]
 
 Times whole buffers of the given configuration -- all its products at once,
 on their concurrent streams, input resident on the device -- with one
 candidate setting at a time, and keeps per product the fastest (coordinate
 descent over the products, the others at their current best).  Timing the
 whole buffer rather than one kernel alone lets the choice see how the
-products share the GPU.  The candidates depend on the kernel the library
+products share the GPU.  The current setting is measured again beside its
+candidates, in interleaved rounds, each setting keeps its fastest time, and
+a candidate replaces the current setting only if it is faster by more than
+--min-gain (2 %; repeated timings of one setting on a GB300 spread by about
+that much).  The candidates depend on the kernel the library
 picked for the product:
 
 - N <= 4096: the CUDA-core kernel k_small with 1, 2, 4, 8 or 16 CTAs per SM
@@ -27,7 +32,6 @@ from __future__ import annotations
 
 import argparse
 import os
-import statistics
 import sys
 import tempfile
 import time
@@ -71,7 +75,7 @@ class Case:
         self.blocks = synth.gaussian_blocks(self.nb, a.nc, a.ntpb, a.np, sigma=20.0, seed=1, nbits=a.nbits)
 
     def run(self, table: dict, path: str) -> tuple[float, list[str]]:
-        """Median ms per buffer over the repetitions, and the kernel class of
+        """Fastest ms per buffer over the repetitions, and the kernel class of
         each product, with `table` as the tuning table."""
         write_table(path, table)
         os.environ[ENV] = path
@@ -93,7 +97,7 @@ class Case:
                 if spec.wait() != 0:
                     raise RuntimeError("processing failed")
                 reps.append(1e3 * (time.perf_counter() - t0) / a.steps)
-            return statistics.median(reps), kinds
+            return min(reps), kinds
         finally:
             spec.close()
 
@@ -117,24 +121,35 @@ def tune(a, log=print) -> tuple[dict, list[str]]:
         base_ms, kinds = case.run(table, tmp.name)
         notes.append(f"library defaults: {base_ms:.3f} ms per buffer, kernels {kinds}")
         log(notes[-1])
-        best_ms = base_ms
         for _ in range(a.passes):
             for i, (nt, na, npol) in enumerate(case.prods):
                 key = case.keys[i]
                 current = dict(table.get(key, {}))
-                for cand in candidates(kinds[i]):
-                    trial = dict(table)
-                    trial[key] = cand
-                    ms, k2 = case.run(trial, tmp.name)
-                    if cand.get("dft") == "tc" and k2[i] != "tc":
-                        log(f"product {i} (Nfft {nt}): no tensor-core DFT for this product, skipped")
+                settings = [current] + [c for c in candidates(kinds[i]) if c != current]
+                best = [float("inf")] * len(settings)
+                for _ in range(a.rounds):
+                    for j, cand in enumerate(settings):
+                        if best[j] is None:
+                            continue
+                        trial = dict(table)
+                        trial[key] = cand
+                        ms, k2 = case.run(trial, tmp.name)
+                        if cand.get("dft") == "tc" and k2[i] != "tc":
+                            log(f"product {i} (Nfft {nt}): no tensor-core DFT for this product, skipped")
+                            best[j] = None
+                            continue
+                        best[j] = min(best[j], ms)
+                for j, cand in enumerate(settings):
+                    if best[j] is None:
                         continue
-                    line = entry_line(key, cand)
-                    log(f"product {i} (Nfft {nt}, Na {na}): {line}: {ms:.3f} ms")
-                    notes.append(f"{line}: {ms:.3f} ms")
-                    if ms < best_ms * (1 - a.min_gain):
-                        best_ms, current = ms, cand
+                    line = entry_line(key, cand) + ("" if j else " (current)")
+                    log(f"product {i} (Nfft {nt}, Na {na}): {line}: {best[j]:.3f} ms")
+                    notes.append(f"{line}: {best[j]:.3f} ms")
+                j = min((j for j in range(len(settings)) if best[j] is not None), key=lambda j: best[j])
+                if best[j] < best[0] * (1 - a.min_gain):
+                    current = settings[j]
                 table[key] = current
+        best_ms, _ = case.run(table, tmp.name)
         notes.append(f"tuned: {best_ms:.3f} ms per buffer ({base_ms / best_ms:.3f}x the defaults)")
         log(notes[-1])
         return {k: v for k, v in table.items() if v}, notes
@@ -156,9 +171,10 @@ def main(argv=None) -> int:
     ap.add_argument("--na", type=int, action="append", required=True)
     ap.add_argument("--npol", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20, help="buffers per timed repetition")
-    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--reps", type=int, default=3, help="timed repetitions per run")
+    ap.add_argument("--rounds", type=int, default=2, help="interleaved runs of every setting")
     ap.add_argument("--passes", type=int, default=1, help="rounds of coordinate descent over the products")
-    ap.add_argument("--min-gain", type=float, default=0.01, help="relative gain a candidate needs over the best")
+    ap.add_argument("--min-gain", type=float, default=0.02, help="relative gain a candidate needs over the current")
     ap.add_argument("--out", default="tuning.txt")
     a = ap.parse_args(argv)
     if len(a.nt) != len(a.na):
