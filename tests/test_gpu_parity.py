@@ -147,8 +147,8 @@ def test_fused_with_incoherent_sum(cuda_device):
 def test_long_integration_3072_spectra(cuda_device, npol):
     # Nint 3072 of 1024-point spectra spanning three 2-block buffers (the
     # production's third product): the per-chunk register sums, the
-    # fixed-order chunk reduction and the accumulation across buffers stay
-    # within the FP32 tolerance of the FP64 oracle.
+    # fixed-order chunk reduction and the compensated accumulation across
+    # buffers stay within the FP32 tolerance of the FP64 oracle.
     Nc, Ntpb = 2, 524288
     c = dict(Nc=Nc, Np=2, Ntpb=Ntpb, nbits=8, nblocks=6, products=[(1024, 3072, npol), (1 << 20, 3, npol)],
              conj=0, fft_dir=1)
