@@ -81,3 +81,52 @@ def test_candidates_follow_the_kernel():
     assert {"dft": "tc"} in tune.candidates("small") and {"dft": "cuda", "ctas": 4} in tune.candidates("tc")
     assert all(c["ring"] > c["lag"] for c in tune.candidates("large_fused"))
     assert all(set(c) == {"ctas"} for c in tune.candidates("large_a"))
+
+
+class FakeCase:
+    """Stands in for the GPU: the time of a buffer is a function of the table."""
+
+    def __init__(self, prods, keys, kinds, cost):
+        self.prods, self.keys, self.kinds, self.cost = prods, keys, kinds, cost
+        self.calls = 0
+
+    def run(self, table, path):
+        self.calls += 1
+        kinds = list(self.kinds)
+        for i, key in enumerate(self.keys):
+            if table.get(key, {}).get("dft") == "cuda":
+                kinds[i] = "small"
+            elif table.get(key, {}).get("dft") == "tc" and self.kinds[i] == "tc":
+                kinds[i] = "tc"
+        return self.cost(table), kinds
+
+
+class Args:
+    passes, rounds, min_gain = 1, 2, 0.02
+
+
+def test_tuner_keeps_a_candidate_only_past_the_threshold():
+    keys = [(1048576, 8, 1), (1024, 8, 1)]
+
+    def cost(table):
+        t = 1.0
+        t += {2: 0.3, 3: 0.05, 4: 0.0, 5: -0.05, 6: -0.01}.get(table.get(keys[0], {}).get("lag", 4), 0.0)
+        c = table.get(keys[1], {})
+        t += 0.05 if c.get("dft") == "cuda" else 0.0
+        t -= 0.01 if c.get("ctas") == 16 else 0.0   # 1 %: below the 2 % threshold
+        return t
+
+    case = FakeCase([(1048576, 51, 1), (1024, 3072, 1)], keys, ["large_fused", "tc"], cost)
+    table, notes = tune.tune(Args(), log=lambda m: None, case=case)
+    assert table == {keys[0]: {"lag": 5, "ring": 10}}
+    assert notes[0].startswith("library defaults") and notes[-1].startswith("tuned:")
+    # every setting twice (the current one included), plus the first and last runs
+    assert case.calls == 2 + 2 * (1 + 5) + 2 * (1 + 6)
+
+
+def test_tuner_skips_tensor_cores_where_the_library_has_none():
+    keys = [(512, 8, -4)]
+    case = FakeCase([(512, 64, -4)], keys, ["small"], lambda table: 0.9 if table.get(keys[0], {}).get("dft") == "tc"
+                    else 1.0)
+    table, notes = tune.tune(Args(), log=lambda m: None, case=case)
+    assert table == {} and not any("dft=tc" in n for n in notes)
