@@ -33,6 +33,7 @@ import ctypes as C
 import json
 import math
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -189,9 +190,38 @@ def cpu_sample_run(nthreads: int, nc_sample: int, reps: int = 1) -> tuple[float,
     return blocks.nbytes / dt / 1e9, dt
 
 
-def cpu_baseline_leg(min_seconds: float = 12.0) -> dict:
+def host_cpu_model() -> str:
+    """The host CPU as /proc/cpuinfo names it (x86: model name; Arm: the
+    implementer and part codes), else the machine type."""
+    try:
+        lines = Path("/proc/cpuinfo").read_text().splitlines()
+    except OSError:
+        return platform.machine()
+    fields = {}
+    for line in lines:
+        if ":" in line:
+            k, v = line.split(":", 1)
+            fields.setdefault(k.strip(), v.strip())
+    if fields.get("model name"):
+        return fields["model name"]
+    if fields.get("CPU implementer") and fields.get("CPU part"):
+        return f"{platform.machine()}, CPU implementer {fields['CPU implementer']}, part {fields['CPU part']}"
+    return platform.machine()
+
+
+def pin_host_threads() -> None:
+    """OpenMP threads bound close together, as the CPU baseline is specified;
+    set before the oracle's OpenMP runtime is loaded (a caller's own
+    setting is kept)."""
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+
+
+def cpu_baseline_leg(min_seconds: float = 12.0, min_seconds_1: float = 3.0) -> dict:
     """The CPU chain on whole buffers of the workload (all 64 channels),
-    repeated until at least min_seconds of CPU work have been timed."""
+    repeated until at least min_seconds of CPU work have been timed, on all
+    host threads; then on one thread over 4 channels of a buffer for at
+    least min_seconds_1."""
+    pin_host_threads()
     from oracle import oracle as O
     threads = O.lib().cpu_max_threads()
     cpu_sample_run(threads, NC)  # warm-up (page-in, thread pool)
@@ -201,9 +231,20 @@ def cpu_baseline_leg(min_seconds: float = 12.0) -> dict:
         secs += dt
         reps += 1
     v = reps * 2 * BLOCK_BYTES / secs / 1e9
+    nc1 = 4
+    cpu_sample_run(1, nc1)
+    reps1, secs1 = 0, 0.0
+    while secs1 < min_seconds_1:
+        _, dt = cpu_sample_run(1, nc1)
+        secs1 += dt
+        reps1 += 1
+    v1 = reps1 * 2 * BLOCK_BYTES * nc1 / NC / secs1 / 1e9
     return {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"{reps} whole buffers (64 channels x 2 blocks, 256 MiB RAW each), all three products, "
-                      f"total power, {secs:.1f} s"}
+                      f"total power, {secs:.1f} s",
+            "one_thread": {"value": v1, "unit": "GB/s", "cores": 1,
+                           "sample": f"{reps1} x {nc1} channels of a buffer, {secs1:.1f} s"},
+            "cpu_model": host_cpu_model(), "omp_proc_bind": os.environ.get("OMP_PROC_BIND", "")}
 
 
 def ingest_leg(nbuf: int = 8) -> dict:
@@ -358,6 +399,7 @@ def run_reference(args, rank, world):
     """CPU restatement of the chain (kind "port") with all host threads."""
     if rank != 0:
         return 0
+    pin_host_threads()
     from oracle import oracle as O
     threads = O.lib().cpu_max_threads()
     # one step = one whole buffer (64 channels x 2 blocks, about 0.5 s on 16
@@ -378,7 +420,8 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded complex Gaussian int8)",
         "config": {"workload": WORKLOAD, "npolout": 1, "parallelism": "host threads"},
-        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample,
+                         "cpu_model": host_cpu_model(), "omp_proc_bind": os.environ.get("OMP_PROC_BIND", "")},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
