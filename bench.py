@@ -50,6 +50,9 @@ SIGMA = 20.0
 E2E_REPS = 5
 BLOCK_BYTES = NC * NTPB * NP * 2
 WORKLOAD = "production shape: 64 ch x 2 pol int8, Ntpb 524288 (128 MiB blocks), Nfft 2^20/8/1024, Nint 51/128/3072"
+# The same config object on both arms (native and reference).
+CONFIG = {"workload": WORKLOAD, "npolout": 1, "step": "one 2-block input buffer (256 MiB RAW)",
+          "l2": "inputs larger than L2 (256 MiB per step)"}
 
 
 def products(npol):
@@ -247,6 +250,54 @@ def cpu_baseline_leg(min_seconds: float = 12.0, min_seconds_1: float = 3.0) -> d
             "cpu_model": host_cpu_model(), "omp_proc_bind": os.environ.get("OMP_PROC_BIND", "")}
 
 
+def cufft_reference_leg(blocks, steps: int, warmup: int, ours_wall_ms: dict) -> dict:
+    """The reference's own GPU library (rawspec_gpu.cu, cuFFT with its load
+    and store callbacks, compiled unchanged for sm_103a) on the same GPU and
+    workload, in a child process: per-buffer wall clock of
+    rawspec_start_processing + rawspec_wait_for_completion with the buffer
+    on the device, no dump callback.  ours_wall_ms: the native library's
+    per-buffer time measured the same way in this process."""
+    from oracle import ref_build, ref_gpu
+    try:
+        lib = ref_build.build_gpu()
+    except RuntimeError as e:
+        return {"unavailable": f"reference GPU build failed: {str(e).splitlines()[0]}"}
+    if lib is None:
+        return {"unavailable": "the reference's GPU sources are not present"}
+    jobs = [(dict(Nc=NC, Np=NP, Ntpb=NTPB, nbits=8, products=[list(p) for p in products(npol)], fft_dir=1,
+                  mode="time", steps=steps, warmup=warmup), blocks) for npol in (1, 4)]
+    try:
+        outs = ref_gpu.run_in_child(jobs)
+    except RuntimeError as e:
+        return {"unavailable": f"reference run failed: {str(e)[-300:]}"}
+    res = {"unit": "GB/s", "timing": "wall clock per buffer of rawspec_start_processing + "
+                                     "rawspec_wait_for_completion, input resident, no dump callback, median of "
+                                     f"{steps} after {warmup} warm-up buffers; both libraries measured the same way",
+           "cufft_version": str(outs[0]["cufft_version"]), "build": "rawspec_gpu.cu unchanged, nvcc -dc for "
+           "sm_103a, static cuFFT (oracle/ref_build.py)"}
+    for npol, out in zip((1, 4), outs):
+        ms = 1e3 * float(statistics.median(out["seconds"]))
+        key = "npolout1" if npol == 1 else "npolout4"
+        res[key] = {"value": 2 * BLOCK_BYTES / (ms / 1e3) / 1e9, "ms_per_step": ms,
+                    "ms_p99": 1e3 * float(sorted(out["seconds"])[max(0, int(0.99 * len(out["seconds"])) - 1)]),
+                    "native_ms_per_step": ours_wall_ms[npol],
+                    "native_speedup": ms / ours_wall_ms[npol]}
+    res["value"] = res["npolout1"]["value"]
+    return res
+
+
+def cpu_baseline_subprocess() -> dict:
+    """cpu_baseline_leg in a child process of its own (no CUDA, no torch)."""
+    res = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--cpu-leg"], capture_output=True, text=True,
+                         cwd=str(ROOT), timeout=900)
+    lines = [l for l in res.stdout.splitlines() if l.startswith("{")]
+    if res.returncode != 0 or not lines:
+        raise RuntimeError(f"CPU baseline leg failed:\n{res.stdout[-2000:]}\n{res.stderr[-2000:]}")
+    out = json.loads(lines[-1])
+    out["process"] = "fresh child process, before any GPU work"
+    return out
+
+
 def ingest_leg(nbuf: int = 8) -> dict:
     """GUPPI RAW files -> librawspec -> SIGPROC filterbank files at the
     production shape: a two-file stem of 2 * nbuf blocks (128 MiB each) in
@@ -419,7 +470,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded complex Gaussian int8)",
-        "config": {"workload": WORKLOAD, "npolout": 1, "parallelism": "host threads"},
+        "config": dict(CONFIG), "parallelism": "host threads",
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample,
                          "cpu_model": host_cpu_model(), "omp_proc_bind": os.environ.get("OMP_PROC_BIND", "")},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -434,9 +485,9 @@ def run_native(args, rank, world, local_rank):
 
     from rawspec_gb300 import api, synth
 
-    # the CPU baseline first, on an otherwise idle host (after the GPU legs it
-    # measured up to 40 % lower in the same process)
-    cpu = cpu_baseline_leg() if rank == 0 and world == 1 and not args.no_cpu else None
+    # the CPU baseline first, on an otherwise idle host, in a fresh process
+    # (after the GPU legs it measured up to 40 % lower in the same process)
+    cpu = cpu_baseline_subprocess() if rank == 0 and world == 1 and not args.no_cpu else None
 
     torch.cuda.set_device(local_rank)
     group = RankGroup(world)
@@ -491,11 +542,19 @@ def run_native(args, rank, world, local_rank):
             t, n = spec.profile(k)
             prof[name] = (t, n)
         spec.set_profiling(False)
+        # per-buffer wall clock of start_processing + wait_for_completion, the
+        # way the reference build is timed (cufft_reference)
+        wall = []
+        for _ in range(args.steps):
+            ts = time.perf_counter()
+            if lib.rawspec_start_processing(cp, 1) != 0 or lib.rawspec_wait_for_completion(cp) != 0:
+                raise RuntimeError("start/wait failed")
+            wall.append(1e3 * (time.perf_counter() - ts))
         # end-to-end through the C-ABI from pinned host blocks: K steps of the
         # reference CLI's per-buffer sequence (rawspec.c:1012-1014), timed
         # five times (host jitter moves single runs); the median is reported,
         # every sample is kept
-        nbuf = args.warmup + 2 * args.steps  # buffers processed so far
+        nbuf = args.warmup + 3 * args.steps  # buffers processed so far
         for _ in range(args.warmup):
             spec.copy_and_start()
             spec.wait()
@@ -531,7 +590,8 @@ def run_native(args, rank, world, local_rank):
         results[npol] = dict(ms=ms, ms_serial=ms_serial, prof=prof, launches=launches, clocks=clocks, e2e_s=e2e_s,
                              e2e_samples=[whole_job_gbs(world, 2 * BLOCK_BYTES, args.steps, x) for x in reps],
                              step_p50=float(np.percentile(step_ms, 50)), step_p99=float(np.percentile(step_ms, 99)),
-                             d2h=d2h / args.steps, device_bytes=int(lib.rawspec_gb300_device_bytes(cp)))
+                             d2h=d2h / args.steps, device_bytes=int(lib.rawspec_gb300_device_bytes(cp)),
+                             wall_ms=float(statistics.median(wall)))
         spec.close()
 
     r = results[1]
@@ -581,9 +641,7 @@ def run_native(args, rank, world, local_rank):
         "metric": "RAW-in GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded complex Gaussian int8, sigma 20)",
-        "config": {"workload": WORKLOAD, "npolout": 1, "step": "one 2-block input buffer (256 MiB RAW)",
-                   "l2": "inputs larger than L2 (256 MiB per step, resident)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": dict(CONFIG), "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": step_bytes,
                 "d2h_bytes_per_step": int(r["d2h"]), "samples": r["e2e_samples"],
                 "buffer_ms_p50": r["step_p50"], "buffer_ms_p99": r["step_p99"],
@@ -606,6 +664,9 @@ def run_native(args, rank, world, local_rank):
     }
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu
+    if rank == 0 and world == 1 and not args.no_cufft:
+        line["cufft_reference"] = cufft_reference_leg(blocks, args.steps, args.warmup,
+                                                      {p: results[p]["wall_ms"] for p in (1, 4)})
     if rank == 0 and world == 1 and not args.no_ingest:
         line["ingest"] = ingest_leg()
     if rank == 0 and world == 1 and not args.no_serve:
@@ -625,8 +686,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-ingest", action="store_true", help="skip the RAW-file ingest leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-mix leg")
+    ap.add_argument("--no-cufft", action="store_true", help="skip the reference cuFFT-build leg")
+    ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.cpu_leg:
+        print(json.dumps(cpu_baseline_leg()), flush=True)
+        return 0
     rank, world, local_rank = rank_info()
     if args.impl == "reference":
         return run_reference(args, rank, world)

@@ -57,3 +57,24 @@ def int4_blocks(nblocks: int, Nc: int, Ntpb: int, Np: int = 2, Nant: int = 1, se
 def weights(Nant: int, seed: int = 5, lo: float = 0.5, hi: float = 1.5) -> np.ndarray:
     rng = np.random.Generator(np.random.PCG64(seed))
     return rng.uniform(lo, hi, size=Nant).astype(np.float32)
+
+
+def gaussian_buffer_cuda(index: int, nblocks: int, Nc: int, Ntpb: int, Np: int = 2, sigma: float = 20.0,
+                         seed: int = 1, device: int = 0) -> np.ndarray:
+    """Blocks index*nblocks ... index*nblocks + nblocks - 1 of a seeded stream
+    of complex Gaussian 8-bit voltages (sigma per component, rounded half to
+    even and clipped to [-128, 127]), drawn on the GPU with torch's
+    counter-based generator, one seed per block, so that any process on the
+    same GPU model and torch version draws the same bytes.  For inputs too
+    large to generate on the host (the production shape over many buffers).
+    Returns uint8 [nblocks, block_bytes] in host memory."""
+    import torch
+    dev = torch.device("cuda", device)
+    out = np.empty((nblocks, Nc * Ntpb * Np * 2), dtype=np.uint8)
+    g = torch.Generator(device=dev)
+    for j in range(nblocks):
+        g.manual_seed(seed * 1000003 + index * nblocks + j)
+        v = torch.randn((Nc, Ntpb, Np, 2), generator=g, device=dev, dtype=torch.float32) * sigma
+        v = torch.round(v).clamp_(-128, 127).to(torch.int8)
+        out[j] = v.view(torch.uint8).reshape(-1).cpu().numpy()
+    return out
