@@ -65,6 +65,12 @@ static_assert(fused_k<POL_TP>() >= 2 && fused_k<POL_FULL>() >= 2, "an item must 
 #ifndef RSG_FUSED_DISCARD
 #define RSG_FUSED_DISCARD 1
 #endif
+// Both polarisations of a tile transformed together as packed pairs (the
+// f32x2 instructions), their exchanges passing the re and then the im pairs
+// through one buffer; 0: one polarisation after the other.
+#ifndef RSG_FUSED_PACKED
+#define RSG_FUSED_PACKED 1
+#endif
 constexpr long long kSpinLimit = 1ll << 24;         // polls of a counter (~2 s with back-off)
 constexpr long long kMbarCycles = 4000000000ll;     // ~2 s of SM clocks for a stage copy
 
@@ -444,12 +450,36 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         ph ^= 1u << buf;
         const int tile = it.titem * K + t;
         const int n1 = tile * C + col;
+        const uint32_t* words = reinterpret_cast<const uint32_t*>(sb) + ((tile * C) & 3) + col;
+#if RSG_FUSED_PACKED
+        // both polarisations in lockstep on the packed instructions
+        cpair v[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) {
+          float2 smp[2];
+          Unpack<FMT_I8, 2>::run(words[(j + T * m) * F::CW], smp);
+          v[m] = pack2(smp[0], smp[1]);
+        }
+        __syncthreads();  // the buffer becomes the exchange buffer; tile t-1 is done
+        if (t > 0) refill(t - 1);
+        const float2 w0 = tw[j * C + col];  // W_N^(n1 j)
+        float2* dst = scr + n1;
+        GroupFFT<N2, R, 2>::template run_packed<true>(v, j, sb + (size_t)col * F::GSA, 0, twA, Sync{});
+#pragma unroll
+        for (int m = 0; m < R; ++m) {
+          const int k2 = j + m * T;
+          // W_N^(n1 k2) = W_N^(n1 j) W_N^(n1 m T)
+          const float2 twk = m == 0 ? w0 : cmul(w0, tw[(T + m) * C + col]);
+          const cpair x = pmul(v[m], twk);
+          st_f2_hint(dst + (size_t)k2 * N1, lane0(x), pol_last);
+          st_f2_hint(dst + ((size_t)N2 + k2) * N1, lane1(x), pol_last);
+        }
+#else
         // polarisation 0 unpacked; polarisation 1 kept as packed bytes, two
         // samples per register, while polarisation 0 is transformed
         float2 v[1][R];
         uint32_t p1[R / 2];
         {
-          const uint32_t* words = reinterpret_cast<const uint32_t*>(sb) + ((tile * C) & 3) + col;
           uint32_t prev = 0;
 #pragma unroll
           for (int m = 0; m < R; ++m) {
@@ -486,6 +516,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
             st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[0][m], twk), pol_last);
           }
         }
+#endif
       }
       publish(doneA + it.slab, K);
       refill(K - 1);
@@ -510,11 +541,61 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
       for (int t = 0; t < K; ++t) {
         const int tile = it.titem * K + t;
         const int k2 = tile * C + row;
-        // Polarisation 0, then 1; total power accumulates |X|^2 of each, the
-        // cross-pol modes keep X0 while X1 is transformed.
         float2 x0[POL != POL_TP ? R : 1];
         float tp[POL == POL_TP ? R : 1];
         float2 v[1][R];
+#if RSG_FUSED_PACKED
+        // Both polarisations (stage 2t in buffer 0, stage 2t+1 in buffer 1)
+        // into registers as packed pairs, transformed in lockstep with the
+        // exchanges in buffer 1; buffer 0 is refilled before the transform,
+        // buffer 1 after it.
+        {
+          float2* sb0 = stg;
+          float2* sb1 = stg + F::XCH;
+          cpair vp[R];
+          mbar_wait(&mbar[0], ph & 1u, err);
+          ph ^= 1u;
+#pragma unroll
+          for (int m = 0; m < R; ++m) v[0][m] = sb0[(size_t)row * F::GSB + j + m * T];
+          mbar_wait(&mbar[1], (ph >> 1) & 1u, err);
+          ph ^= 2u;
+#pragma unroll
+          for (int m = 0; m < R; ++m) vp[m] = pack2(v[0][m], sb1[(size_t)row * F::GSB + j + m * T]);
+#if RSG_FUSED_DISCARD
+          {
+            const char* rows0 = reinterpret_cast<const char*>(scr + (size_t)tile * C * N1);
+            const char* rows1 = reinterpret_cast<const char*>(scr + ((size_t)N2 + (size_t)tile * C) * N1);
+            constexpr int kLines = F::BYTES_B / 128;
+#pragma unroll 1
+            for (int l = tid; l < kLines; l += kFusedTPB) {
+              discard_l2(rows0 + (size_t)l * 128);
+              discard_l2(rows1 + (size_t)l * 128);
+            }
+          }
+#endif
+          // the previous tile's output copy must have read the staging area
+          if (TOUT && tid == 0) bulk_wait_read();
+          __syncthreads();  // both stage buffers are read
+          refill(2 * t);
+          GroupFFT<N1, R, 2>::template run_packed<true>(vp, j, sb1 + (size_t)row * F::GSB, 0, twB, Sync{});
+          refill(2 * t + 1);
+          if constexpr (POL == POL_TP) {
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+              const float2 pw = f2fma(vp[m].im, vp[m].im, f2mul(vp[m].re, vp[m].re));
+              tp[m] = pw.x + pw.y;
+            }
+          } else {
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+              x0[m] = lane0(vp[m]);
+              v[0][m] = lane1(vp[m]);
+            }
+          }
+        }
+#else
+        // Polarisation 0, then 1; total power accumulates |X|^2 of each, the
+        // cross-pol modes keep X0 while X1 is transformed.
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
           const int s = 2 * t + q;
@@ -552,6 +633,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
             }
           }
         }
+#endif
         if constexpr (TOUT) {
           // Shifted bin k2 + N2*((k1 + N1/2) mod N1): staged as
           // [row (k1 + N1/2) mod N1][k2 - tile*C], then written (first

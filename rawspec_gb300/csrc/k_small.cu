@@ -113,6 +113,12 @@ k_small(SmallLaunch a) {
   for (int m = 0; m < R; ++m)
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[m][p] = 0.0f;
+  // Total power of two polarisations on the packed instructions: one lane
+  // per polarisation, the lanes summed after the last spectrum.
+  constexpr bool kPackedTP = POL == POL_TP && NV == 2 && RSG_PACKED;
+  float2 acc2[kPackedTP ? R : 1];
+#pragma unroll
+  for (int m = 0; m < (kPackedTP ? R : 1); ++m) acc2[m] = make_float2(0.f, 0.f);
 
   float2* my_xch = xch + (size_t)g * NV * smem_padded_len(N);
 
@@ -189,14 +195,26 @@ k_small(SmallLaunch a) {
       GroupFFT<N, R, NV>::run(v, j, my_xch, smem_padded_len(N), tw_s, WarpSync{});
     }
     if (valid) {
+      if constexpr (kPackedTP) {
 #pragma unroll
-      for (int m = 0; m < R; ++m) {
-        float2 x[NV];
+        for (int m = 0; m < R; ++m) {
+          const cpair x = pack2(v[0][m], v[1][m]);
+          acc2[m] = f2fma(x.im, x.im, f2fma(x.re, x.re, acc2[m]));
+        }
+      } else {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) x[q] = v[q][m];
-        detect_acc<POL, NV>(acc[m], x, im_sign);
+        for (int m = 0; m < R; ++m) {
+          float2 x[NV];
+#pragma unroll
+          for (int q = 0; q < NV; ++q) x[q] = v[q][m];
+          detect_acc<POL, NV>(acc[m], x, im_sign);
+        }
       }
     }
+  }
+  if constexpr (kPackedTP) {
+#pragma unroll
+    for (int m = 0; m < R; ++m) acc[m][0] = acc2[m].x + acc2[m].y;
   }
 
   // Reduce across the groups of each set: red[g][p][m][j], the groups'

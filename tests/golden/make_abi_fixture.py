@@ -3,7 +3,8 @@ reference's rawspec_context, obtained by compiling abi_probe.c against the
 reference header rawspec.h (run in a checkout where the reference sources
 are available; the fixture is committed so tests need no reference tree).
 
-usage: python tests/golden/make_abi_fixture.py /path/to/reference
+usage: python tests/golden/make_abi_fixture.py [/path/to/reference]
+(default: the reference tree the recipe oracle/ref_build.py resolves)
 """
 import subprocess
 import sys
@@ -23,4 +24,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, str(HERE.parent.parent))
+    from oracle import ref_build
+    main(sys.argv[1] if len(sys.argv) > 1 else str(ref_build.REFERENCE))

@@ -1,7 +1,7 @@
 """Runs one spectrometer configuration through the C-ABI a few times, for
 profiling a single kernel with Nsight Compute.
 
-usage: python -m rawspec_gb300.profile_case --nc 64 --ntpb 524288 --nt 1048576 --na 51 [--npol 1] [--buffers 2]
+usage: python tests/profile_case.py --nc 64 --ntpb 524288 --nt 1048576 --na 51 [--npol 1] [--buffers 2]
        [--nbits 4|8|16] [--np 1|2] [--nant A --ics] [--copy-each] [--timing]
 
 Input: seeded Gaussian voltages (sigma 20; 4-bit: uniform with per-antenna
@@ -17,7 +17,7 @@ import argparse
 import sys
 from pathlib import Path
 
-sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent))  # the repository root
 
 
 def main() -> int:

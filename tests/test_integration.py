@@ -7,8 +7,10 @@ from pathlib import Path
 
 import pytest
 
+from oracle import ref_build
+
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("RAWSPEC_REFERENCE", "/root/reference"))
+REF = ref_build.REFERENCE  # where the reference tree lies (the recipe under oracle/ resolves it)
 CUDA_INC = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
 CUDA_LIB = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "lib64"
 
