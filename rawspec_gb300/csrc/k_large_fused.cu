@@ -65,12 +65,6 @@ static_assert(fused_k<POL_TP>() >= 2 && fused_k<POL_FULL>() >= 2, "an item must 
 #ifndef RSG_FUSED_DISCARD
 #define RSG_FUSED_DISCARD 1
 #endif
-// Both polarisations of a tile transformed together as packed pairs (the
-// f32x2 instructions), their exchanges passing the re and then the im pairs
-// through one buffer; 0: one polarisation after the other.
-#ifndef RSG_FUSED_PACKED
-#define RSG_FUSED_PACKED 1
-#endif
 constexpr long long kSpinLimit = 1ll << 24;         // polls of a counter (~2 s with back-off)
 constexpr long long kMbarCycles = 4000000000ll;     // ~2 s of SM clocks for a stage copy
 
@@ -121,6 +115,12 @@ struct FusedCfg {
   static constexpr int OFF_TWB = round16(TWA), OFF_STG = OFF_TWB + round16(TWB);
   static constexpr int OFF_TWS = OFF_STG + 2 * XCH, OFF_OUT = OFF_TWS + 2 * TWS;
   static constexpr size_t SMEM = (size_t)(OFF_OUT + OUTS) * sizeof(float2) + 128;  // + alignment slack
+  // Ring layout: the intermediate of a polarisation is stored in blocks of
+  // BK consecutive k2, [k2 / BK][n1][k2 % BK].  With BK = C_B a row tile's
+  // input is one contiguous block (one bulk copy) and a warp's column-tile
+  // store covers whole 128-byte lines (its 32 / C_A values of j span the
+  // block); where a warp spans fewer than C_B values of j, BK = 1 (rows).
+  static constexpr int BK = (CB <= 32 / CA) ? CB : 1;
   static constexpr unsigned BYTES_A = (unsigned)N2 * CW * 4;
   static constexpr unsigned BYTES_TW = (unsigned)(TA + RA) * CA * 8;
   static constexpr unsigned BYTES_B = (unsigned)CB * N1 * 8;
@@ -129,6 +129,12 @@ struct FusedCfg {
   static_assert(N2 % BOXR == 0 && CA % 2 == 0, "tensor boxes must tile the column");
   static_assert(N1 % (2 * BOXO) == 0, "output boxes must not straddle the FFT shift");
 };
+
+// Offset of element (k2, n1) of polarisation q within a ring slot.
+template <int N1, int N2, int BK>
+__device__ __forceinline__ size_t ring_index(int q, int k2, int n1) {
+  return ((size_t)q * N2 + (size_t)(k2 / BK) * BK) * N1 + (size_t)n1 * BK + (k2 % BK);
+}
 
 struct Sync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
@@ -382,8 +388,12 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
       const float2* src =
           a.scratch + (size_t)(it.slab % a.ring) * 2 * N + ((size_t)q * N2 + (size_t)tile * F::CB) * N1;
       mbar_expect_tx(mb, F::BYTES_B);
+      if constexpr (F::BK == F::CB) {
+        bulk_load(dst, src, F::BYTES_B, mb);  // one block [n1][C_B rows]
+      } else {
 #pragma unroll 1
-      for (int r = 0; r < F::CB; ++r) bulk_load(dst + (size_t)r * F::GSB, src + (size_t)r * N1, N1 * 8, mb);
+        for (int r = 0; r < F::CB; ++r) bulk_load(dst + (size_t)r * F::GSB, src + (size_t)r * N1, N1 * 8, mb);
+      }
     }
   };
 
@@ -451,7 +461,6 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         const int tile = it.titem * K + t;
         const int n1 = tile * C + col;
         const uint32_t* words = reinterpret_cast<const uint32_t*>(sb) + ((tile * C) & 3) + col;
-#if RSG_FUSED_PACKED
         // both polarisations in lockstep on the packed instructions
         cpair v[R];
 #pragma unroll
@@ -463,7 +472,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         __syncthreads();  // the buffer becomes the exchange buffer; tile t-1 is done
         if (t > 0) refill(t - 1);
         const float2 w0 = tw[j * C + col];  // W_N^(n1 j)
-        float2* dst = scr + n1;
+        float2* dst = scr;
         GroupFFT<N2, R, 2>::template run_packed<true>(v, j, sb + (size_t)col * F::GSA, 0, twA, Sync{});
 #pragma unroll
         for (int m = 0; m < R; ++m) {
@@ -471,52 +480,9 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
           // W_N^(n1 k2) = W_N^(n1 j) W_N^(n1 m T)
           const float2 twk = m == 0 ? w0 : cmul(w0, tw[(T + m) * C + col]);
           const cpair x = pmul(v[m], twk);
-          st_f2_hint(dst + (size_t)k2 * N1, lane0(x), pol_last);
-          st_f2_hint(dst + ((size_t)N2 + k2) * N1, lane1(x), pol_last);
+          st_f2_hint(dst + ring_index<N1, N2, F::BK>(0, k2, n1), lane0(x), pol_last);
+          st_f2_hint(dst + ring_index<N1, N2, F::BK>(1, k2, n1), lane1(x), pol_last);
         }
-#else
-        // polarisation 0 unpacked; polarisation 1 kept as packed bytes, two
-        // samples per register, while polarisation 0 is transformed
-        float2 v[1][R];
-        uint32_t p1[R / 2];
-        {
-          uint32_t prev = 0;
-#pragma unroll
-          for (int m = 0; m < R; ++m) {
-            const uint32_t wm = words[(j + T * m) * F::CW];
-            float2 smp[2];
-            Unpack<FMT_I8, 2>::run(wm, smp);
-            v[0][m] = smp[0];
-            if (m & 1)
-              p1[m / 2] = __byte_perm(prev, wm, 0x7632);
-            else
-              prev = wm;
-          }
-        }
-        __syncthreads();  // the buffer becomes the exchange buffer; tile t-1 is done
-        if (t > 0) refill(t - 1);
-        const float2 w0 = tw[j * C + col];  // W_N^(n1 j)
-        float2* dst = scr + n1;
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          if (q == 1) {
-#pragma unroll
-            for (int m = 0; m < R; ++m) {
-              float2 smp[1];
-              Unpack<FMT_I8, 1>::run((uint16_t)(m & 1 ? p1[m / 2] >> 16 : p1[m / 2] & 0xffffu), smp);
-              v[0][m] = smp[0];
-            }
-          }
-          GroupFFT<N2, R, 1>::run(v, j, sb + (size_t)col * F::GSA, smem_padded_len(N2), twA, Sync{});
-#pragma unroll
-          for (int m = 0; m < R; ++m) {
-            const int k2 = j + m * T;
-            // W_N^(n1 k2) = W_N^(n1 j) W_N^(n1 m T)
-            const float2 twk = m == 0 ? w0 : cmul(w0, tw[(T + m) * C + col]);
-            st_f2_hint(dst + ((size_t)q * N2 + k2) * N1, cmul(v[0][m], twk), pol_last);
-          }
-        }
-#endif
       }
       publish(doneA + it.slab, K);
       refill(K - 1);
@@ -537,6 +503,11 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
       const int d = (a.slab0 + it.slab) % a.units_per_chan;
       float* obase = a.out + ((size_t)d * NP * a.Nc + c) * N;
       const size_t plane = (size_t)a.Nc * N;
+      // where element n1 of this thread's row sits in a landed stage
+      auto row_slot = [&](int n1) -> size_t {
+        if constexpr (F::BK == C) return (size_t)n1 * C + row;
+        else return (size_t)row * F::GSB + n1;
+      };
 #pragma unroll 1
       for (int t = 0; t < K; ++t) {
         const int tile = it.titem * K + t;
@@ -544,7 +515,6 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         float2 x0[POL != POL_TP ? R : 1];
         float tp[POL == POL_TP ? R : 1];
         float2 v[1][R];
-#if RSG_FUSED_PACKED
         // Both polarisations (stage 2t in buffer 0, stage 2t+1 in buffer 1)
         // into registers as packed pairs, transformed in lockstep with the
         // exchanges in buffer 1; buffer 0 is refilled before the transform,
@@ -556,11 +526,11 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
           mbar_wait(&mbar[0], ph & 1u, err);
           ph ^= 1u;
 #pragma unroll
-          for (int m = 0; m < R; ++m) v[0][m] = sb0[(size_t)row * F::GSB + j + m * T];
+          for (int m = 0; m < R; ++m) v[0][m] = sb0[row_slot(j + m * T)];
           mbar_wait(&mbar[1], (ph >> 1) & 1u, err);
           ph ^= 2u;
 #pragma unroll
-          for (int m = 0; m < R; ++m) vp[m] = pack2(v[0][m], sb1[(size_t)row * F::GSB + j + m * T]);
+          for (int m = 0; m < R; ++m) vp[m] = pack2(v[0][m], sb1[row_slot(j + m * T)]);
 #if RSG_FUSED_DISCARD
           {
             const char* rows0 = reinterpret_cast<const char*>(scr + (size_t)tile * C * N1);
@@ -593,47 +563,6 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
             }
           }
         }
-#else
-        // Polarisation 0, then 1; total power accumulates |X|^2 of each, the
-        // cross-pol modes keep X0 while X1 is transformed.
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          const int s = 2 * t + q;
-          const int buf = s & 1;
-          float2* sb = stg + (size_t)buf * F::XCH;
-          mbar_wait(&mbar[buf], (ph >> buf) & 1u, err);
-          ph ^= 1u << buf;
-#pragma unroll
-          for (int m = 0; m < R; ++m) v[0][m] = sb[(size_t)row * F::GSB + j + m * T];
-#if RSG_FUSED_DISCARD
-          {
-            const char* rows = reinterpret_cast<const char*>(scr + ((size_t)q * N2 + (size_t)tile * C) * N1);
-            constexpr int kLines = F::BYTES_B / 128;
-#pragma unroll 1
-            for (int l = tid; l < kLines; l += kFusedTPB) discard_l2(rows + (size_t)l * 128);
-          }
-#endif
-          // the previous tile's output copy must have read the staging area
-          if (TOUT && q == 0 && tid == 0) bulk_wait_read();
-          __syncthreads();  // the buffer becomes the exchange buffer
-          GroupFFT<N1, R, 1>::run(v, j, sb + (size_t)row * F::GSB, smem_padded_len(N1), twB, Sync{});
-          refill(s);
-          if constexpr (POL == POL_TP) {
-#pragma unroll
-            for (int m = 0; m < R; ++m) {
-              float t1[1] = {q == 0 ? 0.0f : tp[m]};
-              const float2 xx[1] = {v[0][m]};
-              detect_acc<POL_TP, 1>(t1, xx, im_sign);
-              tp[m] = t1[0];
-            }
-          } else {
-            if (q == 0) {
-#pragma unroll
-              for (int m = 0; m < R; ++m) x0[m] = v[0][m];
-            }
-          }
-        }
-#endif
         if constexpr (TOUT) {
           // Shifted bin k2 + N2*((k1 + N1/2) mod N1): staged as
           // [row (k1 + N1/2) mod N1][k2 - tile*C], then written (first
