@@ -110,10 +110,11 @@ int rawspec_gb300_device_bytes_estimate(const rawspec_context *ctx, size_t *byte
  *
  *   d_in     device input, [Nc][samples_per_channel][Np][re,im], Nbps = 8 or
  *            16 bits per component (the layout rawspec_copy_blocks_to_gpu
- *            produces; 4-bit input must be expanded first)
+ *            produces; 4-bit input must be expanded first), aligned to one
+ *            time sample (Np * 2 * Nbps / 8 bytes)
  *   Nt, Na   FFT length (power of two, at most 4096) and spectra per
  *            integration; Nt*Na must divide samples_per_channel
- *   Npolout  1, +4 (full pol) or -4 (Stokes), coerced to 1 unless Np == 2
+ *   Npolout  1, +4 (full pol) or -4 (Stokes; +4 and -4 need Np == 2)
  *   d_out    device output, [Nd][|Npolout|][Nc][Nt] float, FFT-shifted, with
  *            Nd = samples_per_channel / (Nt*Na): the same values
  *            rawspec_start_processing() dumps for such a product
@@ -126,6 +127,9 @@ int rawspec_gb300_device_bytes_estimate(const rawspec_context *ctx, size_t *byte
  * the array's device address (make that first call before any stream capture
  * on that device).  Every call shares the array and it keeps the last call's
  * contents; everything a call reads from it is written by the same call first.
+ * The looked-up address belongs to the device's primary context (the CUDA
+ * runtime's); after cudaDeviceReset the library must be reloaded before this
+ * entry point is used again.
  * Calls that overlap on the GPU (different streams, or another host thread)
  * race on the array and must be serialised by the caller.
  * Returns 0 when the work is queued, 1 on invalid arguments or a CUDA error

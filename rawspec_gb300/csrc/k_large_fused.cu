@@ -146,15 +146,26 @@ __device__ __forceinline__ int load_acquire(const int* p) {
   return v;
 }
 
-// Thread 0 polls until *cnt reaches target (bounded; on time-out it records
-// `code` in the error word and lets the CTA proceed), then the CTA proceeds.
-__device__ __forceinline__ void wait_count(const int* cnt, int target, int* err, int code) {
-  if (threadIdx.x == 0) {
+// A bounded wait that runs out records its code in the error word and sets
+// the CTA's abort flag: from then on the CTA issues no copy, skips every
+// wait, finishes its current work item on whatever the buffers hold (all
+// accesses stay in bounds), drains the copies already in flight and exits.
+__device__ __forceinline__ void set_abort(int* err, int code, int* abort_flag) {
+  atomicExch(err, code);
+  *reinterpret_cast<volatile int*>(abort_flag) = 1;
+}
+__device__ __forceinline__ bool aborted(const int* abort_flag) {
+  return *reinterpret_cast<const volatile int*>(abort_flag) != 0;
+}
+
+// Thread 0 polls until *cnt reaches target (bounded), then the CTA proceeds.
+__device__ __forceinline__ void wait_count(const int* cnt, int target, int* err, int code, int* abort_flag) {
+  if (threadIdx.x == 0 && !aborted(abort_flag)) {
     unsigned ns = 32;
     long long it = 0;
     while (load_acquire(cnt) < target) {
       if (++it > kSpinLimit) {
-        atomicExch(err, code);
+        set_abort(err, code, abort_flag);
         break;
       }
       __nanosleep(ns);
@@ -228,16 +239,18 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* mb, unsigned p
   return ok != 0;
 }
 // Waits for the phase of the given parity to complete (bounded by SM clock
-// cycles; on time-out the error word is set and the CTA carries on).
-__device__ __forceinline__ void mbar_wait(unsigned long long* mb, unsigned parity, int* err) {
-  if (mbar_try_wait(mb, parity)) return;
+// cycles; see set_abort).  Returns false if it ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* mb, unsigned parity) {
+  if (mbar_try_wait(mb, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(mb, parity)) {
-    if (clock64() - t0 > kMbarCycles) {
-      atomicExch(err, 3);
-      return;
-    }
+    if (clock64() - t0 > kMbarCycles) return false;
   }
+  return true;
+}
+__device__ __forceinline__ void mbar_wait(unsigned long long* mb, unsigned parity, int* err, int* abort_flag) {
+  if (aborted(abort_flag)) return;
+  if (!mbar_wait_bounded(mb, parity)) set_abort(err, 3, abort_flag);
 }
 // Orders this CTA's earlier generic-proxy accesses of shared memory before
 // later asynchronous-proxy (copy engine) writes to it.
@@ -334,6 +347,8 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
   __shared__ __align__(8) unsigned long long mbar[2];
   __shared__ long long s_next;
   __shared__ int s_pre;
+  __shared__ int s_abort;
+  __shared__ unsigned s_issued[2];  // stages thread 0 has requested into each buffer
 
   const int tid = threadIdx.x;
   const int S = a.S;
@@ -356,6 +371,8 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
     mbar_init_fence();
     s_next = (long long)atomicAdd(reinterpret_cast<unsigned int*>(next), 1u);
     s_pre = 0;
+    s_abort = 0;
+    s_issued[0] = s_issued[1] = 0;
   }
   for (int i = tid; i < F::TWA; i += kFusedTPB) twA[i] = a.twN2[i];
   for (int i = tid; i < F::TWB; i += kFusedTPB) twB[i] = a.twN1[i];
@@ -366,6 +383,8 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
   // tile's twiddle slices; row stage s: polarisation s%2 of the C_B rows of
   // tile titem*K + s/2, from the ring.
   auto issue_stage = [&](const Item& it, int s, int buf) {
+    if (aborted(&s_abort)) return;
+    ++s_issued[buf];
     float2* dst = stg + (size_t)buf * F::XCH;
     unsigned long long* mb = &mbar[buf];
     if (it.isA) {
@@ -403,8 +422,9 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
     __syncthreads();  // the previous item's s_next / s_pre are written
     const long long item = s_next;
     const int pre = s_pre;
+    const int abort_now = s_abort;
     __syncthreads();
-    if (item >= total) break;
+    if (item >= total || abort_now) break;
     const Item it = decode_item(item, S, a.lag, itemsA, itemsB);
     long long nxt = total;
     if (tid == 0) pre_ok = false;
@@ -446,7 +466,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         issue_stage(it, 0, 0);
         issue_stage(it, 1, 1);
       }
-      if (it.slab >= a.ring) wait_count(doneB + (it.slab - a.ring), tilesB, err, 1);
+      if (it.slab >= a.ring) wait_count(doneB + (it.slab - a.ring), tilesB, err, 1, &s_abort);
       // ---- K column tiles: N2-point FFTs of C_A columns n1 each ------------
       constexpr int R = F::RA, T = F::TA, C = F::CA;
       const int col = tid % C;
@@ -456,7 +476,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
         const int buf = t & 1;
         float2* sb = stg + (size_t)buf * F::XCH;
         const float2* tw = tws + (size_t)buf * F::TWS;  // [T][C] then [R][C]
-        mbar_wait(&mbar[buf], (ph >> buf) & 1u, err);
+        mbar_wait(&mbar[buf], (ph >> buf) & 1u, err, &s_abort);
         ph ^= 1u << buf;
         const int tile = it.titem * K + t;
         const int n1 = tile * C + col;
@@ -488,7 +508,7 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
       refill(K - 1);
     } else {
       if (!pre) {
-        wait_count(doneA + it.slab, tilesA, err, 2);
+        wait_count(doneA + it.slab, tilesA, err, 2, &s_abort);
         if (tid == 0) {
           fence_proxy_async();
           issue_stage(it, 0, 0);
@@ -523,11 +543,11 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
           float2* sb0 = stg;
           float2* sb1 = stg + F::XCH;
           cpair vp[R];
-          mbar_wait(&mbar[0], ph & 1u, err);
+          mbar_wait(&mbar[0], ph & 1u, err, &s_abort);
           ph ^= 1u;
 #pragma unroll
           for (int m = 0; m < R; ++m) v[0][m] = sb0[row_slot(j + m * T)];
-          mbar_wait(&mbar[1], (ph >> 1) & 1u, err);
+          mbar_wait(&mbar[1], (ph >> 1) & 1u, err, &s_abort);
           ph ^= 2u;
 #pragma unroll
           for (int m = 0; m < R; ++m) vp[m] = pack2(v[0][m], sb1[row_slot(j + m * T)]);
@@ -614,7 +634,14 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
     }
     if (tid == 0) s_pre = pre_ok ? 1 : 0;
   }
-  // output copies still in flight complete before the CTA retires
+  // Copies still in flight complete before the CTA retires: after a normal
+  // run every requested stage has been waited for; after an abort, the last
+  // stage requested into each buffer is waited for (bounded; the phases of an
+  // mbarrier complete in order, so the earlier ones are then complete too).
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b)
+      if (s_issued[b] > 0 && !mbar_wait_bounded(&mbar[b], (s_issued[b] - 1) & 1u)) atomicExch(err, 4);
+  }
   if (TOUT && tid == 0) bulk_wait_all();
   // The last CTA to finish zeroes the counters for the next launch (every
   // other CTA has stopped reading them); the error word stays.

@@ -52,7 +52,8 @@ struct TcCfg {
   static constexpr int B_BYTES = (ND / 8) * SBO;
   static constexpr int TW_BYTES = N * 8;      // W_N^(n2 k1) as [k1][n2] float2
   static constexpr int TAB_BYTES = B_BYTES + TW_BYTES;
-  // stage-1 operand | T hi | T lo | DFT operand | twiddles | 2 mbarriers, tensor-memory slot
+  // stage-1 operand | T hi | T lo | DFT operand | twiddles | 2 mbarriers,
+  // tensor-memory slot, 2 commit counters
   static constexpr int SMEM = 3 * A_BYTES + TAB_BYTES + 32;
   static constexpr int TMEM_COLS = 2 * ND;    // stage-1 and stage-2 accumulators
   static constexpr int THREADS = 256;         // two warps per tensor-memory lane quarter
@@ -103,6 +104,7 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
   uint64_t* mb1 = reinterpret_cast<uint64_t*>(sB + C::TAB_BYTES);
   uint64_t* mb2 = mb1 + 1;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mb1 + 2);
+  uint32_t* ncommit = tslot + 1;  // commits issued to mb1 and mb2 (thread 0)
   float* red = reinterpret_cast<float*>(sm);  // reduction area over the operands
 
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -114,6 +116,7 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
   if (tid == 0) {
     tc::mbar_init(mb1, 1);
     tc::mbar_init(mb2, 1);
+    ncommit[0] = ncommit[1] = 0;
   }
   if (warp == 0) {
     tc::tmem_alloc(tslot, C::TMEM_COLS);
@@ -176,6 +179,7 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
       tc::mma_f16(d1, tc::smem_desc(aA1 + ks * 2 * C::LBO, C::LBO, C::SBO),
                   tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC, ks > 0 ? 1u : 0u);
     tc::mma_commit(mb1);
+    ++ncommit[0];
   };
   // T hi x [F hi | F lo] + T lo x F hi (the lo x lo term is below 2^-22)
   auto issue_s2 = [&]() {
@@ -188,6 +192,7 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
       tc::mma_f16(d2, tc::smem_desc(aLo + ks * 2 * C::LBO, C::LBO, C::SBO),
                   tc::smem_desc(bF + ks * 2 * C::LBO, C::LBO, C::SBO), IDESC_HI, 1u);
     tc::mma_commit(mb2);
+    ++ncommit[1];
   };
   auto wait = [&](uint64_t* mb, unsigned& ph) {
     if (!tc::mbar_wait_bounded(mb, ph, kTcWaitCycles)) bad = 1;
@@ -360,7 +365,15 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
     __syncthreads();
   }
 
-  // every tensor-memory load has completed (tcgen05.wait::ld) before the free
+  // No MMA is still running when the tensor memory is freed: after a normal
+  // run every commit has been waited for; after a time-out the issuing
+  // thread waits (bounded) for the last commit of each barrier (the phases
+  // of an mbarrier complete in order).  Every tensor-memory load has
+  // completed (tcgen05.wait::ld) as well.
+  if (tid == 0) {
+    if (ncommit[0] > 0 && !tc::mbar_wait_bounded(mb1, (ncommit[0] - 1) & 1u, kTcWaitCycles)) bad = 1;
+    if (ncommit[1] > 0 && !tc::mbar_wait_bounded(mb2, (ncommit[1] - 1) & 1u, kTcWaitCycles)) bad = 1;
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();

@@ -9,6 +9,7 @@
 // the per-chunk partial sums of the fused small-FFT kernel and its twiddle
 // table -- in the file-scope array below, which every GPU that loads the
 // library holds until the process exits.
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 
@@ -34,6 +35,8 @@ float* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 // Device address of the scratch array on the current device, looked up once
 // per device.  In host code the array's name is only a host-side stand-in.
+// The address belongs to the device's primary context (the one the CUDA
+// runtime uses); it is not looked up again after cudaDeviceReset.
 float* scratch_for_current_device() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
@@ -64,6 +67,21 @@ extern "C" int rawspec_gb300_product_noalloc(const void* d_in, unsigned int Nc, 
     fprintf(stderr, "rawspec_gb300_product_noalloc: invalid arguments\n");
     return 1;
   }
+  if (Npolout != 1 && Npolout != 4 && Npolout != -4) {
+    fprintf(stderr, "rawspec_gb300_product_noalloc: Npolout must be 1, 4 or -4, not %d\n", Npolout);
+    return 1;
+  }
+  if (Npolout != 1 && Np != 2) {
+    fprintf(stderr, "rawspec_gb300_product_noalloc: Npolout %d needs two polarisations\n", Npolout);
+    return 1;
+  }
+  // The kernels read one time sample (all polarisations) as one word.
+  const unsigned word_bytes = Np * 2u * (Nbps / 8u);
+  if ((reinterpret_cast<uintptr_t>(d_in) % word_bytes) != 0 || (reinterpret_cast<uintptr_t>(d_out) % 4) != 0) {
+    fprintf(stderr, "rawspec_gb300_product_noalloc: d_in must be aligned to %u bytes and d_out to 4 bytes\n",
+            word_bytes);
+    return 1;
+  }
   if (!pow2(Nt) || Nt > (unsigned)kMaxNt) {
     fprintf(stderr, "rawspec_gb300_product_noalloc: Nt (%u) must be a power of two no larger than %d\n", Nt, kMaxNt);
     return 1;
@@ -74,12 +92,18 @@ extern "C" int rawspec_gb300_product_noalloc(const void* d_in, unsigned int Nc, 
             samples_per_channel);
     return 1;
   }
+  // integration units (channel x dump) are counted in int by the kernels
+  if ((unsigned long long)Nc * (samples_per_channel / span) > 0x7fffffffULL) {
+    fprintf(stderr, "rawspec_gb300_product_noalloc: too many integrations (%u channels x %llu)\n", Nc,
+            samples_per_channel / span);
+    return 1;
+  }
   float* scratch = scratch_for_current_device();
   if (!scratch) return 1;
   float2* tw = reinterpret_cast<float2*>(scratch + kPartialFloats);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
 
-  const int npol = (Np == 2 && (Npolout == 4 || Npolout == -4)) ? Npolout : 1;
+  const int npol = Npolout;
   SmallLaunch L;
   L.logN = 0;
   while ((1u << L.logN) < Nt) ++L.logN;
