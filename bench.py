@@ -65,11 +65,12 @@ def rank_info():
 
 
 class RankGroup:
-    """Host-side coordination of the replicas of a multi-GPU run: one process
-    per GPU, each with its own context and its own data (the channels of
-    different ranks are independent, so no data moves between ranks).  Only
-    the barrier around the timed region and the max over ranks of the timings
-    go through the process group (gloo, on the host)."""
+    """Host-side coordination of a multi-GPU run: one process per GPU, each
+    with the context of its channel shard of the observation and its own data
+    (the channels of different ranks are independent, so no data moves
+    between ranks).  Only the barrier around the timed region and the max
+    over ranks of the timings go through the process group (gloo, on the
+    host)."""
 
     def __init__(self, world: int):
         self.world = world
@@ -496,7 +497,11 @@ def run_native(args, rank, world, local_rank):
     blocks = synth.gaussian_blocks(2, NC, NTPB, NP, sigma=SIGMA, seed=1 + rank)
     results = {}
     for npol in (1, 4):
-        spec = api.Spectrometer(NC, NP, NTPB, NBITS, products(npol), gpu_index=local_rank, collect=False)
+        # one observation of 64 x N channels, sharded by channel: this rank's
+        # context holds its 64 (rawspec_gb300_shard_context)
+        spec = api.Spectrometer(NC * world, NP, NTPB, NBITS, products(npol), gpu_index=local_rank, collect=False,
+                                shard=(rank, world))
+        assert spec.ctx.Nc == NC
         lib = spec.lib
         cp = C.byref(spec.ctx)
         stream = torch.cuda.ExternalStream(spec.stream(), device=local_rank)
@@ -641,7 +646,9 @@ def run_native(args, rank, world, local_rank):
         "metric": "RAW-in GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded complex Gaussian int8, sigma 20)",
-        "config": dict(CONFIG), "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+        "config": dict(CONFIG),
+        "parallelism": (f"channel shards x{world}: one observation of {NC * world} channels, {NC} per GPU, "
+                        "no data exchanged") if world > 1 else "single GPU",
         "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": step_bytes,
                 "d2h_bytes_per_step": int(r["d2h"]), "samples": r["e2e_samples"],
                 "buffer_ms_p50": r["step_p50"], "buffer_ms_p99": r["step_p99"],

@@ -92,6 +92,41 @@ typedef struct {
  * by rawspec_initialize and the device-memory estimate; no CUDA calls. */
 int rawspec_gb300_tune_lookup(unsigned nfft, int nbits, int npolout, rawspec_gb300_tune *t);
 
+/* ---- channel shards: one observation over several GPUs -------------------
+ * A shard is the range [k0, k0 + nk) of channels-within-antenna of every
+ * antenna (channel c of antenna a is a * Nc/Nant + c in the GUPPI block), so
+ * that all antennas of a channel, which the incoherent sum combines, stay on
+ * one GPU; shards exchange nothing.  One process per GPU runs a context of
+ * Nant * nk channels for its shard.  Host code only (no CUDA calls). */
+
+/* Shard `rank` of `world` of Nc channels in Nant antennas: nearly equal
+ * contiguous ranges of the Nc/Nant channels-within-antenna.  0 on success,
+ * 1 on invalid arguments or an empty shard (world > Nc/Nant). */
+int rawspec_gb300_shard_range(unsigned int Nc, unsigned int Nant, int rank, int world,
+                              unsigned int *k0, unsigned int *nk);
+
+/* Fills *shard with the client fields of *full for shard `rank` of `world`
+ * (Nc = Nant * nk, channel batching off, library-allocated host blocks; the
+ * weights pointer and the dump callback are shared).  The caller then calls
+ * rawspec_initialize(shard).  0 on success, 1 on invalid arguments. */
+int rawspec_gb300_shard_context(const rawspec_context *full, int rank, int world,
+                                rawspec_context *shard);
+
+/* Copies the shard's channels of one host block of the full observation
+ * (Nc channels of channel_bytes each) into a host block of the shard
+ * context.  0 on success, 1 on invalid arguments. */
+int rawspec_gb300_shard_fill_block(const void *full_block, unsigned int Nc, unsigned int Nant,
+                                   unsigned int k0, unsigned int nk, size_t channel_bytes,
+                                   void *shard_block);
+
+/* Puts one dump of a shard into the dump buffer of the full observation:
+ * rows = Nd * |Npolout| rows of channels, Nt floats per channel; ics = 0 for
+ * h_pwrbuf ([rows][Nc][Nt] in the full buffer), 1 for h_icsbuf
+ * ([rows][Nc/Nant][Nt]).  0 on success, 1 on invalid arguments. */
+int rawspec_gb300_shard_place_dump(const float *shard_dump, unsigned int Nc, unsigned int Nant,
+                                   unsigned int k0, unsigned int nk, unsigned int rows,
+                                   unsigned int Nt, int ics, float *full_dump);
+
 /* Device memory rawspec_initialize() would allocate for this context (the
  * same validation and kernel configuration, nothing allocated; the context
  * itself is not modified).  Needs the CUDA device gpu_index.  0 on success,

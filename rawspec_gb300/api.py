@@ -122,6 +122,14 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
             "rawspec_gb300_device_bytes": (C.c_size_t, [P]),
             "rawspec_gb300_product_kernel": (C.c_int, [P, C.c_int]),
             "rawspec_gb300_tune_lookup": (C.c_int, [C.c_uint, C.c_int, C.c_int, C.POINTER(TuneEntry)]),
+            "rawspec_gb300_shard_range": (C.c_int, [C.c_uint, C.c_uint, C.c_int, C.c_int, C.POINTER(C.c_uint),
+                                                   C.POINTER(C.c_uint)]),
+            "rawspec_gb300_shard_context": (C.c_int, [P, C.c_int, C.c_int, P]),
+            "rawspec_gb300_shard_fill_block": (C.c_int, [C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
+                                                        C.c_size_t, C.c_void_p]),
+            "rawspec_gb300_shard_place_dump": (C.c_int, [C.POINTER(C.c_float), C.c_uint, C.c_uint, C.c_uint,
+                                                        C.c_uint, C.c_uint, C.c_uint, C.c_int,
+                                                        C.POINTER(C.c_float)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -169,16 +177,60 @@ def make_context(Nc: int, Np: int, Ntpb: int, nbits: int, products: Sequence[tup
     return ctx
 
 
+def shard_range(Nc: int, Nant: int, rank: int, world: int) -> tuple[int, int]:
+    """rawspec_gb300_shard_range: (k0, nk), the channels-within-antenna of a shard."""
+    k0, nk = C.c_uint(), C.c_uint()
+    if load_library().rawspec_gb300_shard_range(Nc, Nant, rank, world, C.byref(k0), C.byref(nk)) != 0:
+        raise ValueError(f"no shard {rank} of {world} for {Nc} channels in {Nant} antennas")
+    return k0.value, nk.value
+
+
+def shard_fill_block(full_block: np.ndarray, Nc: int, Nant: int, k0: int, nk: int) -> np.ndarray:
+    """rawspec_gb300_shard_fill_block: the shard's channels of one full host block."""
+    full_block = np.ascontiguousarray(full_block, dtype=np.uint8)
+    cb = full_block.size // Nc
+    out = np.empty(Nant * nk * cb, dtype=np.uint8)
+    if load_library().rawspec_gb300_shard_fill_block(full_block.ctypes.data, Nc, Nant, k0, nk, cb,
+                                                      out.ctypes.data) != 0:
+        raise ValueError("shard_fill_block: invalid arguments")
+    return out
+
+
+def shard_place_dump(shard_dump: np.ndarray, full_dump: np.ndarray, Nc: int, Nant: int, k0: int, nk: int, Nt: int,
+                     ics: bool = False) -> None:
+    """rawspec_gb300_shard_place_dump: writes one shard dump into full_dump
+    (float32, the full observation's dump layout) in place."""
+    sd = np.ascontiguousarray(shard_dump, dtype=np.float32)
+    assert full_dump.dtype == np.float32 and full_dump.flags["C_CONTIGUOUS"]
+    per_row = (1 if ics else Nant) * nk * Nt
+    rows = sd.size // per_row
+    Pf = C.POINTER(C.c_float)
+    if load_library().rawspec_gb300_shard_place_dump(sd.ctypes.data_as(Pf), Nc, Nant, k0, nk, rows, Nt,
+                                                      1 if ics else 0, full_dump.ctypes.data_as(Pf)) != 0:
+        raise ValueError("shard_place_dump: invalid arguments")
+
+
 class Spectrometer:
-    """A librawspec context plus the host-side loop of a typical client."""
+    """A librawspec context plus the host-side loop of a typical client.
+    With shard=(rank, world) the context is that shard of the observation
+    (rawspec_gb300_shard_context): Nant * nk of its Nc channels."""
 
     def __init__(self, Nc: int, Np: int, Ntpb: int, nbits: int, products: Sequence[tuple[int, int, int]], *,
                  Nant: int = 1, Nbc: int = 0, Nb: int = 0, conj: int = 0, gpu_index: int = 0,
-                 weights: Sequence[float] | None = None, collect: bool = True):
+                 weights: Sequence[float] | None = None, collect: bool = True,
+                 shard: tuple[int, int] | None = None):
         self.lib = load_library()
         self.nbits_in = nbits
         self.ctx = make_context(Nc, Np, Ntpb, nbits, products, Nant=Nant, Nbc=Nbc, Nb=Nb, conj=conj,
                                 gpu_index=gpu_index, weights=weights)
+        self.full_Nc, self.k0, self.nk = Nc, 0, Nc // max(Nant, 1)
+        if shard is not None:
+            full = self.ctx
+            self.ctx = RawspecContext()
+            if self.lib.rawspec_gb300_shard_context(C.byref(full), shard[0], shard[1], C.byref(self.ctx)) != 0:
+                raise ValueError(f"no shard {shard} of {Nc} channels in {Nant} antennas")
+            self.ctx._weights_keepalive = getattr(full, "_weights_keepalive", None)  # type: ignore[attr-defined]
+            self.k0, self.nk = shard_range(Nc, Nant, shard[0], shard[1])
         self.collect = collect
         self.dumps: list[list[np.ndarray]] = [[] for _ in products]
         self.ics: list[list[np.ndarray]] = [[] for _ in products]

@@ -3,9 +3,10 @@
 The spectrometer shards by coarse channel with no exchange: every channel's
 products depend on that channel's voltages only, and the incoherent sum on
 the antennas of one channel, which a rank keeps together.  Two ranks launched
-by torch.distributed.run each process their share (the FP32 CPU chain stands
-in for the GPU); their dumps, put side by side, must equal a single-process
-run bit for bit.  The workers also run bench.py's rank coordination.
+by torch.distributed.run each take their shard through the library's shard
+API and process it (the FP32 CPU chain stands in for the GPU); their dumps,
+put back with rawspec_gb300_shard_place_dump, must equal a single-process run
+bit for bit.  The workers also run bench.py's rank coordination.
 """
 from __future__ import annotations
 
@@ -24,19 +25,13 @@ sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 import multirank_worker as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
-from rawspec_gb300 import synth  # noqa: E402
+from rawspec_gb300 import api, synth  # noqa: E402
 
 
 def _free_port() -> int:
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
         return s.getsockname()[1]
-
-
-def _split(a: np.ndarray, np_out: int, nc: int, nt: int) -> np.ndarray:
-    """[ndumps, Nd*|P|*Nc*Nt] -> [ndumps, Nd, |P|, Nc, Nt]."""
-    nd = a.shape[1] // (np_out * nc * nt)
-    return a.reshape(a.shape[0], nd, np_out, nc, nt)
 
 
 def test_two_rank_channel_shards_match_single_process(tmp_path):
@@ -51,26 +46,19 @@ def test_two_rank_channel_shards_match_single_process(tmp_path):
     blocks = synth.gaussian_blocks(W.NB, W.NC, W.NTPB, W.NP, sigma=16.0, seed=7)
     cfg = O.make_cfg(W.NC, W.NP, W.NTPB, W.NB, 8, W.PRODUCTS, Nant=W.NANT, weights=W.WEIGHTS)
     outs, icss = O.run_cpu(cfg, blocks, nthreads=1)
-    nca = W.NC // W.NANT
-    covered = []
+    placed = [np.zeros_like(o) for o in outs]
+    placed_ics = [np.zeros_like(s) for s in icss]
+    covered = 0
     for rank in range(2):
         got = np.load(tmp_path / f"rank{rank}.npz")
-        chans = list(got["chans"])
-        covered += chans
+        k0, nk = int(got["k0"]), int(got["nk"])
+        covered += nk
         for i, (nt, _, npo) in enumerate(W.PRODUCTS):
-            full = _split(outs[i], abs(npo), W.NC, nt)[:, :, :, chans, :]
-            part = _split(got[f"out{i}"], abs(npo), len(chans), nt)
-            np.testing.assert_array_equal(part, full)
-            cw = [c for c in chans if c < nca]  # channel-within-antenna indices of this rank
-            full_ics = _split(icss[i], abs(npo), nca, nt)[:, :, :, cw, :]
-            part_ics = _split(got[f"ics{i}"], abs(npo), len(cw), nt)
-            np.testing.assert_array_equal(part_ics, full_ics)
-    assert sorted(covered) == list(range(W.NC))
-
-
-@pytest.mark.parametrize("world", [1, 2, 3])
-def test_shards_cover_channels_once(world):
-    seen = []
-    for r in range(world):
-        seen += W.shard_channels(r, world)
-    assert sorted(seen) == list(range(W.NC))
+            assert got[f"out{i}"].shape[0] == outs[i].shape[0]
+            for d in range(outs[i].shape[0]):
+                api.shard_place_dump(got[f"out{i}"][d], placed[i][d], W.NC, W.NANT, k0, nk, nt)
+                api.shard_place_dump(got[f"ics{i}"][d], placed_ics[i][d], W.NC, W.NANT, k0, nk, nt, ics=True)
+    assert covered == W.NC // W.NANT
+    for i in range(len(W.PRODUCTS)):
+        np.testing.assert_array_equal(placed[i], outs[i])
+        np.testing.assert_array_equal(placed_ics[i], icss[i])
