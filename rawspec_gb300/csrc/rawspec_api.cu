@@ -207,11 +207,13 @@ bool graphs_wanted(const GpuCtx* g) {
 }
 
 // Which products of 8-bit input run their DFT on the tensor cores (k_tc)
-// rather than in k_small: by default the total-power products of N = 1024
-// and 4096, where k_tc is faster alone (2 % and 13 %) and leaves FMA and
-// issue slots to concurrent CUDA-core kernels; the cross-pol modes stay on
-// k_small (k_tc is as fast alone but slows a mixed step with the fused
-// kernel), N = 256 too (k_tc is slower).  RAWSPEC_GB300_TENSOR_DFT=1 at
+// rather than in k_small: by default the total-power products of N = 1024,
+// where k_tc is faster alone (227 against 233 us per 256 MiB buffer) and
+// leaves FMA and issue slots to concurrent CUDA-core kernels.  Since k_small
+// runs both polarisations on the packed f32x2 instructions it is the faster
+// one at N = 4096 (299 against 339 us) and N = 256; the cross-pol modes stay
+// on k_small (k_tc is as fast alone but slows a mixed step with the fused
+// kernel).  RAWSPEC_GB300_TENSOR_DFT=1 at
 // initialisation selects k_tc for every case it supports (N = 256, 1024,
 // 4096, all modes up to 1024), =0 for none.  Without the variable, a
 // tuning-table entry's dft= decides before the default.
@@ -220,7 +222,7 @@ bool tensor_dft_wanted(int logN, int pol, const rawspec_gb300_tune& t) {
   if (v && v[0] == '0') return false;
   if (v && v[0] == '1') return true;
   if (t.dft >= 0) return t.dft == 1;
-  return (logN == 10 || logN == 12) && pol == POL_TP;
+  return logN == 10 && pol == POL_TP;
 }
 
 // Tuning-table entry of product i of a validated context (unset values if
