@@ -287,6 +287,86 @@ def cufft_reference_leg(blocks, steps: int, warmup: int, ours_wall_ms: dict) -> 
     return res
 
 
+def c3_leg(steps: int, warmup: int, peak_gbs: float) -> dict:
+    """The batched multi-antenna 4-bit configuration: 4 antennas x 16 coarse
+    channels, 2 pols, 4-bit samples (uniform in [-8, 7] scaled by a gain per
+    antenna), Ntpb 262144, products Nfft 4096 / Nint 64 and Nfft 64 / Nint
+    1024 in full Stokes, weighted incoherent sum over the antennas.  One step
+    = one block (32 MiB of packed RAW input, 64 MiB once expanded).
+      value  RAW-in GB/s, expanded block resident: K x rawspec_start_processing,
+             CUDA events on the library's stream;
+      e2e    wall clock of K x (rawspec_wait_for_completion +
+             rawspec_copy_blocks_to_gpu_and_start_processing with the 4-bit
+             expansion) from pinned host blocks;
+      roofline  the dominant kernel's bytes per launch (the expanded input
+             it reads + its integrated output) over its CUDA-event time."""
+    import torch
+
+    from rawspec_gb300 import api, synth
+    nant, nc, ntpb = 4, 64, 262144
+    prods = [(4096, 64, -4), (64, 1024, -4)]
+    blocks, _gains = synth.int4_blocks(1, nc, ntpb, 2, Nant=nant, seed=3)
+    w = list(synth.weights(nant, seed=5))
+    raw = nc * ntpb * 2  # packed bytes of one block
+    with api.Spectrometer(nc, 2, ntpb, 4, prods, Nant=nant, weights=w, collect=False) as spec:
+        lib, cp = spec.lib, C.byref(spec.ctx)
+        stream = torch.cuda.ExternalStream(spec.stream())
+        spec.load_blocks(blocks)
+        spec.copy_to_gpu()
+        for _ in range(warmup):
+            spec.start()
+        spec.wait()
+        l0 = spec.kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            if lib.rawspec_start_processing(cp, 1) != 0:
+                raise RuntimeError("start_processing failed")
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        launches = (spec.kernel_launches() - l0) / steps
+        spec.wait()
+        spec.reset_profile()
+        spec.set_profiling(True)
+        for _ in range(steps):
+            spec.start()
+        spec.wait()
+        prof = {name: spec.profile(k) for k, name in enumerate(api.KERNEL_CLASS_NAMES)}
+        spec.set_profiling(False)
+        ts = time.perf_counter()
+        for _ in range(steps):
+            if lib.rawspec_wait_for_completion(cp) != 0 or \
+                    lib.rawspec_copy_blocks_to_gpu_and_start_processing(cp, 1, 1, 1) != 0:
+                raise RuntimeError("copy/start failed")
+        if lib.rawspec_wait_for_completion(cp) != 0:
+            raise RuntimeError("wait failed")
+        e2e_s = (time.perf_counter() - ts) / steps
+        kinds = [spec.product_kernel(i) for i in range(len(prods))]
+    cls = max((k for k in prof if k not in ("d2h", "h2d")), key=lambda k: prof[k][0])
+    t_ms, n = prof[cls]
+    # bytes the dominant kernel must move per launch: the expanded input
+    # (2 bytes per complex sample and polarisation) + the integrated output
+    # of its product (4 planes x Nc x Nt floats per integration)
+    expanded = nc * ntpb * 2 * 2
+    out_bytes = {i: 4 * nc * nt * 4 * (ntpb // (nt * na)) for i, (nt, na, _p) in enumerate(prods)}
+    prod_of = [i for i, k in enumerate(kinds) if k == cls]
+    alg = expanded + (sum(out_bytes[i] for i in prod_of) / max(len(prod_of), 1))
+    per_launch_ms = t_ms / n if n else None
+    achieved = alg / (per_launch_ms / 1e3) / 1e9 if per_launch_ms else None
+    return {"workload": "4 antennas x 16 ch, 4-bit, Ntpb 262144, Nfft 4096/64, Nint 64/1024, Stokes, weighted "
+                        "incoherent sum; one block (32 MiB packed) per step",
+            "value": raw / (ms / 1e3) / 1e9, "unit": "GB/s", "ms_per_step": ms, "steps": steps,
+            "gpu_launches_per_step": launches,
+            "e2e": {"value": raw / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": raw},
+            "kernels": kinds,
+            "kernel_ms_per_step": {k: v[0] / steps for k, v in prof.items() if v[1]},
+            "roofline": {"bound": "hbm", "kernel": f"k_{cls}", "achieved": achieved, "peak": peak_gbs,
+                         "unit": "GB/s", "frac": achieved / peak_gbs if achieved else None,
+                         "bytes_per_launch": alg}}
+
+
 def cpu_baseline_subprocess() -> dict:
     """cpu_baseline_leg in a child process of its own (no CUDA, no torch)."""
     res = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--cpu-leg"], capture_output=True, text=True,
@@ -674,6 +754,8 @@ def run_native(args, rank, world, local_rank):
     if rank == 0 and world == 1 and not args.no_cufft:
         line["cufft_reference"] = cufft_reference_leg(blocks, args.steps, args.warmup,
                                                       {p: results[p]["wall_ms"] for p in (1, 4)})
+    if rank == 0 and world == 1 and not args.no_c3:
+        line["c3"] = c3_leg(args.steps, args.warmup, peak)
     if rank == 0 and world == 1 and not args.no_ingest:
         line["ingest"] = ingest_leg()
     if rank == 0 and world == 1 and not args.no_serve:
@@ -694,6 +776,7 @@ def main():
     ap.add_argument("--no-ingest", action="store_true", help="skip the RAW-file ingest leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-mix leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the reference cuFFT-build leg")
+    ap.add_argument("--no-c3", action="store_true", help="skip the multi-antenna 4-bit leg")
     ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
