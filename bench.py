@@ -496,7 +496,8 @@ def serving_leg(njobs: int = 256, rate: float = 40.0, budget: float = 120e9) -> 
                 "buffers": int(st.buffers), "dumps": int(st.dumps), "peak_active_jobs": int(st.peak_active),
                 "peak_device_bytes": int(st.peak_used),
                 "buffer_ms_p50": st.buffer_p50_ms, "buffer_ms_p99": st.buffer_p99_ms,
-                "dump_ms_p50": st.dump_p50_ms, "dump_ms_p99": st.dump_p99_ms}
+                "dump_ms_p50": st.dump_p50_ms, "dump_ms_p99": st.dump_p99_ms,
+                "group_calls": int(st.group_calls)}
 
     arrivals = served(True)
     burst = served(False)

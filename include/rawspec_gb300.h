@@ -92,6 +92,22 @@ typedef struct {
  * by rawspec_initialize and the device-memory estimate; no CUDA calls. */
 int rawspec_gb300_tune_lookup(unsigned nfft, int nbits, int npolout, rawspec_gb300_tune *t);
 
+/* One input buffer of each of n initialised contexts on one device, already
+ * copied to the device (rawspec_copy_blocks_to_gpu): the work that
+ * rawspec_start_processing(ctxs[k], fft_dirs[k]) queues for each, except that
+ * the fused small-FFT kernel launches (FFT lengths up to 4096 on the CUDA
+ * cores) of the contexts that share a kernel configuration (FFT length,
+ * sample format, polarisations, output mode) run as one grid of up to 8
+ * launches.  Each context's dumps, callbacks and integration state are its
+ * own, as with separate calls; a context appears at most once.  Contexts on
+ * different devices or with profiling on are processed one after another.
+ * 0 on success, 1 on error. */
+int rawspec_gb300_start_processing_group(rawspec_context *const *ctxs, const int *fft_dirs, int n);
+
+/* Kernel launches of this context that also carried other contexts'
+ * buffers (rawspec_gb300_start_processing_group). */
+unsigned long long rawspec_gb300_shared_launches(rawspec_context *ctx);
+
 /* ---- channel shards: one observation over several GPUs -------------------
  * A shard is the range [k0, k0 + nk) of channels-within-antenna of every
  * antenna (channel c of antenna a is a * Nc/Nant + c in the GUPPI block), so

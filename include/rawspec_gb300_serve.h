@@ -89,6 +89,8 @@ typedef struct {
   int peak_active;
   long long buffers, dumps;
   double buffer_p50_ms, buffer_p99_ms, dump_p50_ms, dump_p99_ms;  /* over all jobs */
+  long long group_calls;  /* times several jobs' buffers were started together, their
+                             launches of one kernel configuration sharing a grid */
 } rawspec_gb300_server_stats;
 
 int rawspec_gb300_server_get_stats(rawspec_gb300_server *s, rawspec_gb300_server_stats *st);

@@ -122,6 +122,8 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
             "rawspec_gb300_device_bytes": (C.c_size_t, [P]),
             "rawspec_gb300_product_kernel": (C.c_int, [P, C.c_int]),
             "rawspec_gb300_tune_lookup": (C.c_int, [C.c_uint, C.c_int, C.c_int, C.POINTER(TuneEntry)]),
+            "rawspec_gb300_start_processing_group": (C.c_int, [C.POINTER(P), C.POINTER(C.c_int), C.c_int]),
+            "rawspec_gb300_shared_launches": (C.c_ulonglong, [P]),
             "rawspec_gb300_shard_range": (C.c_int, [C.c_uint, C.c_uint, C.c_int, C.c_int, C.POINTER(C.c_uint),
                                                    C.POINTER(C.c_uint)]),
             "rawspec_gb300_shard_context": (C.c_int, [P, C.c_int, C.c_int, P]),
@@ -175,6 +177,16 @@ def make_context(Nc: int, Np: int, Ntpb: int, nbits: int, products: Sequence[tup
         ctx.Naws = len(weights)
         ctx.Aws = C.cast(w, C.POINTER(C.c_float))
     return ctx
+
+
+def start_group(specs: Sequence["Spectrometer"], fft_dirs: Sequence[int] | None = None) -> None:
+    """rawspec_gb300_start_processing_group over the specs' contexts (each
+    spec's buffer already copied to the device)."""
+    n = len(specs)
+    arr = (C.POINTER(RawspecContext) * n)(*[C.pointer(sp.ctx) for sp in specs])
+    dirs = (C.c_int * n)(*(fft_dirs if fft_dirs is not None else [RAWSPEC_FORWARD_FFT] * n))
+    if load_library().rawspec_gb300_start_processing_group(arr, dirs, n) != 0:
+        raise RuntimeError("rawspec_gb300_start_processing_group failed")
 
 
 def shard_range(Nc: int, Nant: int, rank: int, world: int) -> tuple[int, int]:
@@ -344,6 +356,10 @@ class Spectrometer:
 
     def kernel_launches(self) -> int:
         return int(self.lib.rawspec_gb300_kernel_launches(C.byref(self.ctx)))
+
+    def shared_launches(self) -> int:
+        """Launches of this context that also carried other contexts' buffers."""
+        return int(self.lib.rawspec_gb300_shared_launches(C.byref(self.ctx)))
 
     def stream(self) -> int:
         return int(self.lib.rawspec_gb300_stream(C.byref(self.ctx)) or 0)

@@ -59,6 +59,17 @@ struct SmallLaunch {
 // range.  partial_floats receives the scratch the launch needs (0 if none).
 int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats, int pipe_groups = 1);
 cudaError_t small_launch(const SmallLaunch& L, cudaStream_t s);
+// Up to kSmallGroupMax launches of the same kernel configuration (FFT length,
+// sample format, polarisations, mode) in one grid, e.g. the buffers of
+// several contexts: the entries keep their own buffers, units and splits.
+constexpr int kSmallGroupMax = 8;
+struct SmallGroup {
+  SmallLaunch e[kSmallGroupMax];
+  int end[kSmallGroupMax];  // prefix sums of the entries' grids
+  int n = 0;
+};
+bool small_same_kernel(const SmallLaunch& a, const SmallLaunch& b);
+cudaError_t small_launch_group(const SmallLaunch* L, int n, cudaStream_t s);
 // Raises the kernel's dynamic shared-memory limit on the current device.
 cudaError_t small_prepare(const SmallLaunch& L);
 

@@ -69,9 +69,11 @@ __host__ __device__ constexpr size_t small_smem_bytes() {
   return tw + (xch > red ? xch : red);
 }
 
+// The kernel body for CTA `bid` of launch `a` (k_small: one launch;
+// k_small_group: several launches of the same configuration, e.g. the
+// buffers of several jobs, in one grid).
 template <int N, int FMT, int NV, int POL>
-__global__ void __launch_bounds__(SmallCfg<N, PolOut<POL>::NP>::TPB, SmallCfg<N, PolOut<POL>::NP>::MINB)
-k_small(SmallLaunch a) {
+__device__ __forceinline__ void small_body(const SmallLaunch& a, const int bid) {
   constexpr int NP = PolOut<POL>::NP;
   using C = SmallCfg<N, NP>;
   constexpr int R = C::R, T = C::T, G = C::G, TPB = C::TPB;
@@ -95,8 +97,8 @@ k_small(SmallLaunch a) {
   const int gps = G / a.sets;           // groups per set
   const int set = g / gps;
   const int gi = g % gps;
-  const int ublock = blockIdx.x / a.chunks;
-  const int chunk = blockIdx.x % a.chunks;
+  const int ublock = bid / a.chunks;
+  const int chunk = bid % a.chunks;
   const int unit = a.unit0 + ublock * a.sets + set;
   const int s_begin = chunk * a.spc;
   const int s_end = min(a.M, s_begin + a.spc);
@@ -247,6 +249,22 @@ k_small(SmallLaunch a) {
   }
 }
 
+template <int N, int FMT, int NV, int POL>
+__global__ void __launch_bounds__(SmallCfg<N, PolOut<POL>::NP>::TPB, SmallCfg<N, PolOut<POL>::NP>::MINB)
+k_small(const __grid_constant__ SmallLaunch a) {
+  small_body<N, FMT, NV, POL>(a, blockIdx.x);
+}
+
+// Several launches of one configuration in one grid: CTA b belongs to the
+// launch k whose range [end[k-1], end[k]) holds it.
+template <int N, int FMT, int NV, int POL>
+__global__ void __launch_bounds__(SmallCfg<N, PolOut<POL>::NP>::TPB, SmallCfg<N, PolOut<POL>::NP>::MINB)
+k_small_group(const __grid_constant__ SmallGroup g) {
+  int k = 0;
+  while (k + 1 < g.n && (int)blockIdx.x >= g.end[k]) ++k;
+  small_body<N, FMT, NV, POL>(g.e[k], (int)blockIdx.x - (k ? g.end[k - 1] : 0));
+}
+
 // Finalisation of chunked units: fixed-order sum of the chunks' partials,
 // SNORM scale and FFT-shifted store.
 __global__ void k_finalize(FinalizeLaunch a) {
@@ -307,52 +325,65 @@ SmallInfo small_info_dyn(int logN, int nv, int pol) {
   }
 }
 
+int small_grid(const SmallLaunch& L) { return ((L.unit_count + L.sets - 1) / L.sets) * L.chunks; }
+
 // op: 0 launch, 1 allow the dynamic shared memory, 2 also report the
-// resident CTAs per SM in *occ.
+// resident CTAs per SM in *occ, 3 launch the group *grp (entries of L's
+// configuration).
 template <int N, int FMT, int NV, int POL>
-cudaError_t launch_t(const SmallLaunch& L, cudaStream_t s, int op, int* occ) {
+cudaError_t launch_t(const SmallLaunch& L, cudaStream_t s, int op, int* occ, const SmallGroup* grp) {
   auto k = k_small<N, FMT, NV, POL>;
+  if (op == 3) {
+    auto kg = k_small_group<N, FMT, NV, POL>;
+    cudaError_t e = cudaFuncSetAttribute(kg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+    if (e != cudaSuccess) return e;
+    const int grid = grp->end[grp->n - 1];
+    if (grid < 1) return cudaSuccess;
+    kg<<<grid, SmallCfg<N, PolOut<POL>::NP>::TPB, L.smem, s>>>(*grp);
+    return cudaGetLastError();
+  }
   if (op != 0) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
     if (e != cudaSuccess || op == 1) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k, SmallCfg<N, PolOut<POL>::NP>::TPB, L.smem);
   }
-  const int grid = ((L.unit_count + L.sets - 1) / L.sets) * L.chunks;
+  const int grid = small_grid(L);
   if (grid < 1) return cudaSuccess;
   k<<<grid, SmallCfg<N, PolOut<POL>::NP>::TPB, L.smem, s>>>(L);
   return cudaGetLastError();
 }
 
 template <int N, int FMT>
-cudaError_t launch_pol(const SmallLaunch& L, cudaStream_t s, int op, int* occ) {
-  if (L.nv == 1) return launch_t<N, FMT, 1, POL_TP>(L, s, op, occ);
+cudaError_t launch_pol(const SmallLaunch& L, cudaStream_t s, int op, int* occ, const SmallGroup* grp) {
+  if (L.nv == 1) return launch_t<N, FMT, 1, POL_TP>(L, s, op, occ, grp);
   switch (L.pol) {
-    case POL_FULL: return launch_t<N, FMT, 2, POL_FULL>(L, s, op, occ);
-    case POL_STOKES: return launch_t<N, FMT, 2, POL_STOKES>(L, s, op, occ);
-    default: return launch_t<N, FMT, 2, POL_TP>(L, s, op, occ);
+    case POL_FULL: return launch_t<N, FMT, 2, POL_FULL>(L, s, op, occ, grp);
+    case POL_STOKES: return launch_t<N, FMT, 2, POL_STOKES>(L, s, op, occ, grp);
+    default: return launch_t<N, FMT, 2, POL_TP>(L, s, op, occ, grp);
   }
 }
 
 template <int N>
-cudaError_t launch_fmt(const SmallLaunch& L, cudaStream_t s, int op, int* occ) {
-  return L.fmt == FMT_I16 ? launch_pol<N, FMT_I16>(L, s, op, occ) : launch_pol<N, FMT_I8>(L, s, op, occ);
+cudaError_t launch_fmt(const SmallLaunch& L, cudaStream_t s, int op, int* occ, const SmallGroup* grp) {
+  return L.fmt == FMT_I16 ? launch_pol<N, FMT_I16>(L, s, op, occ, grp) : launch_pol<N, FMT_I8>(L, s, op, occ, grp);
 }
 
-cudaError_t small_dispatch(const SmallLaunch& L, cudaStream_t s, int op, int* occ = nullptr) {
+cudaError_t small_dispatch(const SmallLaunch& L, cudaStream_t s, int op, int* occ = nullptr,
+                           const SmallGroup* grp = nullptr) {
   switch (L.logN) {
-    case 0: return launch_fmt<1>(L, s, op, occ);
-    case 1: return launch_fmt<2>(L, s, op, occ);
-    case 2: return launch_fmt<4>(L, s, op, occ);
-    case 3: return launch_fmt<8>(L, s, op, occ);
-    case 4: return launch_fmt<16>(L, s, op, occ);
-    case 5: return launch_fmt<32>(L, s, op, occ);
-    case 6: return launch_fmt<64>(L, s, op, occ);
-    case 7: return launch_fmt<128>(L, s, op, occ);
-    case 8: return launch_fmt<256>(L, s, op, occ);
-    case 9: return launch_fmt<512>(L, s, op, occ);
-    case 10: return launch_fmt<1024>(L, s, op, occ);
-    case 11: return launch_fmt<2048>(L, s, op, occ);
-    case 12: return launch_fmt<4096>(L, s, op, occ);
+    case 0: return launch_fmt<1>(L, s, op, occ, grp);
+    case 1: return launch_fmt<2>(L, s, op, occ, grp);
+    case 2: return launch_fmt<4>(L, s, op, occ, grp);
+    case 3: return launch_fmt<8>(L, s, op, occ, grp);
+    case 4: return launch_fmt<16>(L, s, op, occ, grp);
+    case 5: return launch_fmt<32>(L, s, op, occ, grp);
+    case 6: return launch_fmt<64>(L, s, op, occ, grp);
+    case 7: return launch_fmt<128>(L, s, op, occ, grp);
+    case 8: return launch_fmt<256>(L, s, op, occ, grp);
+    case 9: return launch_fmt<512>(L, s, op, occ, grp);
+    case 10: return launch_fmt<1024>(L, s, op, occ, grp);
+    case 11: return launch_fmt<2048>(L, s, op, occ, grp);
+    case 12: return launch_fmt<4096>(L, s, op, occ, grp);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -425,6 +456,24 @@ int small_configure(SmallLaunch& L, int target_ctas, size_t* partial_floats, int
 
 cudaError_t small_prepare(const SmallLaunch& L) { return small_dispatch(L, nullptr, 1); }
 cudaError_t small_launch(const SmallLaunch& L, cudaStream_t s) { return small_dispatch(L, s, 0); }
+
+bool small_same_kernel(const SmallLaunch& a, const SmallLaunch& b) {
+  return a.logN == b.logN && a.fmt == b.fmt && a.nv == b.nv && (a.nv == 1 || a.pol == b.pol) && a.smem == b.smem;
+}
+
+cudaError_t small_launch_group(const SmallLaunch* L, int n, cudaStream_t s) {
+  if (n < 1 || n > kSmallGroupMax) return cudaErrorInvalidValue;
+  SmallGroup g;
+  g.n = n;
+  int end = 0;
+  for (int k = 0; k < n; ++k) {
+    if (!small_same_kernel(L[0], L[k])) return cudaErrorInvalidValue;
+    g.e[k] = L[k];
+    end += std::max(0, small_grid(L[k]));
+    g.end[k] = end;
+  }
+  return small_dispatch(L[0], s, 3, nullptr, &g);
+}
 
 cudaError_t finalize_launch(const FinalizeLaunch& L, cudaStream_t s) {
   const long long total = (long long)L.n_units * L.np * L.N;

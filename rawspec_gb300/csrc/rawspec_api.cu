@@ -112,12 +112,14 @@ struct GpuCtx {
   float* d_aws = nullptr;
   Product prod[MAX_OUTPUTS];
   unsigned inbuf_count = 0;
+  int cur_mode[MAX_OUTPUTS] = {0};  // write / add of each product for the buffer being queued
   bool caller_managed = false;
   unsigned registered = 0;  // caller blocks examined (and page-locked unless they already were) so far
   std::vector<char> locked_here;  // per caller block: page-locked by this library (unlocked at cleanup)
   DumpCb cb[MAX_OUTPUTS];
   size_t device_bytes = 0;
   unsigned long long launches = 0;
+  unsigned long long shared_launches = 0;  // launches that also carried other contexts' buffers
   // profiling
   bool profiling = false;
   std::vector<EventPair> pending;
@@ -550,10 +552,22 @@ int launch_finalize(rawspec_context* ctx, GpuCtx* g, const Product& P, float* ou
   return 0;
 }
 
+// A k_small launch held back so that it can share one grid with launches
+// of other contexts (rawspec_gb300_start_processing_group).
+struct DeferredSmall {
+  rawspec_context* ctx;
+  GpuCtx* g;
+  int product;
+  SmallLaunch L;
+  float* out;
+};
+
 // Queues product i's kernels for the channels [c0, c1) of the buffer.  With
 // compensated integration the buffers after an integration's first write
-// their sums to the staging plane.
-int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse, int c0, int c1) {
+// their sums to the staging plane.  With `defer`, a k_small launch over all
+// channels is recorded there instead (with its finalisation).
+int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse, int c0, int c1,
+                   std::vector<DeferredSmall>* defer = nullptr) {
   Product& P = g->prod[i];
   const bool staged = P.kahan && mode == ACC_ADD;
   float* const out = staged ? P.d_stage : P.d_out;
@@ -590,6 +604,9 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
     if (c1 - c0 < (int)ctx->Nc) {  // a channel group: the finer split
       L.chunks = L.chunks_pipe;
       L.spc = L.spc_pipe;
+    } else if (defer && !g->profiling) {
+      defer->push_back(DeferredSmall{ctx, g, i, L, out});
+      return 0;
     }
     {
       ProfScope ps(g, RAWSPEC_GB300_K_SMALL, P.stream);
@@ -638,11 +655,12 @@ int launch_product(rawspec_context* ctx, GpuCtx* g, int i, int mode, int inverse
   return 0;
 }
 
-// Processes one input buffer: each product's kernels, on the product's own
+// Queues one input buffer's kernels: each product's, on the product's own
 // stream, over `ngroups` channel groups (group k waits for ready[k] when
-// given), then the dumps of the products whose integration completes, also
-// on the product's stream; the context stream joins all of them.
-int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, const cudaEvent_t* ready) {
+// given).  With `defer`, k_small launches over all channels are recorded
+// there instead of queued (the caller queues them, then buffer_finish).
+int buffer_launches(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, const cudaEvent_t* ready,
+                    std::vector<DeferredSmall>* defer) {
   const int inverse = fft_dir <= 0 ? 1 : 0;
   g->inbuf_count++;
   RSG_CUDA(cudaEventRecord(g->ev_fork, g->stream));
@@ -651,7 +669,7 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
     P.stream = g->profiling ? g->stream : P.own_stream;
     RSG_CUDA(cudaStreamWaitEvent(P.stream, g->ev_fork, 0));
   }
-  int mode[MAX_OUTPUTS];
+  int* mode = g->cur_mode;
   for (unsigned i = 0; i < ctx->No; i++)
     mode[i] = ((g->inbuf_count - 1) % g->prod[i].Nis == 0) ? ACC_WRITE : ACC_ADD;
   for (int grp = 0; grp < ngroups; grp++) {
@@ -660,9 +678,17 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
     if (c1 <= c0) continue;
     for (unsigned i = 0; i < ctx->No; i++) {
       if (ready) RSG_CUDA(cudaStreamWaitEvent(g->prod[i].stream, ready[grp], 0));
-      if (launch_product(ctx, g, (int)i, mode[i], inverse, c0, c1)) return 1;
+      if (launch_product(ctx, g, (int)i, mode[i], inverse, c0, c1, defer)) return 1;
     }
   }
+  return 0;
+}
+
+// After a buffer's kernels: the compensated integration merge, and the dumps
+// of the products whose integration completes, each on the product's
+// stream; the context stream joins all of them.
+int buffer_finish(rawspec_context* ctx, GpuCtx* g) {
+  const int* mode = g->cur_mode;
   for (unsigned i = 0; i < ctx->No; i++) {
     Product& P = g->prod[i];
     if (P.kahan) {
@@ -704,6 +730,66 @@ int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, co
     }
     RSG_CUDA(cudaEventRecord(P.ev_join, P.stream));
     RSG_CUDA(cudaStreamWaitEvent(g->stream, P.ev_join, 0));
+  }
+  return 0;
+}
+
+
+// Processes one input buffer (buffer_launches, then buffer_finish).
+int process_buffer(rawspec_context* ctx, GpuCtx* g, int fft_dir, int ngroups, const cudaEvent_t* ready) {
+  if (buffer_launches(ctx, g, fft_dir, ngroups, ready, nullptr)) return 1;
+  return buffer_finish(ctx, g);
+}
+
+// Queues the deferred k_small launches of several contexts: launches of the
+// same kernel configuration share one grid (up to kSmallGroupMax), issued on
+// the first one's product stream after every member's stream has reached
+// it; each member's stream then continues after the shared launch with its
+// own finalisation.
+int launch_deferred(std::vector<DeferredSmall>& d) {
+  std::vector<char> done(d.size(), 0);
+  for (size_t a = 0; a < d.size(); a++) {
+    if (done[a]) continue;
+    std::vector<size_t> mem{a};
+    done[a] = 1;
+    for (size_t b = a + 1; b < d.size() && (int)mem.size() < kSmallGroupMax; b++)
+      if (!done[b] && small_same_kernel(d[a].L, d[b].L)) {
+        mem.push_back(b);
+        done[b] = 1;
+      }
+    Product& Pa = d[a].g->prod[d[a].product];
+    cudaStream_t st = Pa.stream;
+    std::vector<SmallLaunch> Ls;
+    for (size_t m : mem) {
+      Ls.push_back(d[m].L);
+      if (m == a) continue;
+      GpuCtx* gm = d[m].g;
+      cudaEvent_t ev = take_event(gm);
+      if (!ev) return 1;
+      RSG_CUDA(cudaEventRecord(ev, gm->prod[d[m].product].stream));
+      RSG_CUDA(cudaStreamWaitEvent(st, ev, 0));
+      gm->free_events.push_back(ev);  // the wait has taken the event's state
+    }
+    if (mem.size() == 1) {
+      RSG_CUDA(small_launch(Ls[0], st));
+    } else {
+      RSG_CUDA(small_launch_group(Ls.data(), (int)Ls.size(), st));
+      cudaEvent_t done_ev = take_event(d[a].g);
+      if (!done_ev) return 1;
+      RSG_CUDA(cudaEventRecord(done_ev, st));
+      for (size_t m : mem)
+        if (m != a) RSG_CUDA(cudaStreamWaitEvent(d[m].g->prod[d[m].product].stream, done_ev, 0));
+      d[a].g->free_events.push_back(done_ev);
+    }
+    for (size_t m : mem) {
+      DeferredSmall& e = d[m];
+      e.g->launches++;  // every member's context counts the launch it took part in
+      if (mem.size() > 1) e.g->shared_launches++;
+      Product& P = e.g->prod[e.product];
+      if (e.L.chunks > 1 && launch_finalize(e.ctx, e.g, P, e.out, e.L.unit0, e.L.unit_count, e.L.chunks,
+                                            e.L.units_per_chan, e.L.mode, e.L.inverse, e.L.scale))
+        return 1;
+    }
   }
   return 0;
 }
@@ -1296,6 +1382,37 @@ int rawspec_start_processing(rawspec_context* ctx, int fft_dir) {
   return 0;
 }
 
+// One buffer of each of several contexts (e.g. the jobs of a server): each
+// context's work as rawspec_start_processing queues it, except that the
+// k_small launches of the contexts that share a kernel configuration run as
+// one grid.  Contexts on different devices, or with profiling on, are
+// processed one after another instead.
+int rawspec_gb300_start_processing_group(rawspec_context* const* ctxs, const int* fft_dirs, int n) {
+  if (!ctxs || !fft_dirs || n < 1) return 1;
+  GpuCtx* g0 = G(ctxs[0]);
+  if (!g0) return 1;
+  bool plain = n == 1;
+  for (int k = 0; k < n; k++) {
+    GpuCtx* g = ctxs[k] ? G(ctxs[k]) : nullptr;
+    if (!g) return 1;
+    for (int m = 0; m < k; m++)
+      if (ctxs[m] == ctxs[k]) return 1;
+    if (g->device != g0->device || g->profiling) plain = true;
+  }
+  if (plain) {
+    for (int k = 0; k < n; k++)
+      if (rawspec_start_processing(ctxs[k], fft_dirs[k])) return 1;
+    return 0;
+  }
+  std::vector<DeferredSmall> d;
+  for (int k = 0; k < n; k++)
+    if (buffer_launches(ctxs[k], G(ctxs[k]), fft_dirs[k], 1, nullptr, &d)) return 1;
+  if (launch_deferred(d)) return 1;
+  for (int k = 0; k < n; k++)
+    if (buffer_finish(ctxs[k], G(ctxs[k]))) return 1;
+  return 0;
+}
+
 // The copy of a full buffer is split into channel groups on a copy stream;
 // the kernels of group k start as soon as its copy has landed, so the
 // host-to-device transfer overlaps the processing.  The call returns, like
@@ -1435,6 +1552,11 @@ int rawspec_gb300_reset_profile(rawspec_context* ctx) {
     g->prof_n[k] = 0;
   }
   return 0;
+}
+
+unsigned long long rawspec_gb300_shared_launches(rawspec_context* ctx) {
+  GpuCtx* g = G(ctx);
+  return g ? g->shared_launches : 0;
 }
 
 unsigned long long rawspec_gb300_kernel_launches(rawspec_context* ctx) {

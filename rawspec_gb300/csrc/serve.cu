@@ -25,6 +25,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -119,12 +120,20 @@ struct rawspec_gb300_server {
   size_t used = 0, peak_used = 0;
   int active = 0, peak_active = 0;
   bool stop = false;
+  // several ready jobs' buffers started together (RAWSPEC_GB300_SERVE_GROUP=0: never)
+  bool group = true;
+  long long group_calls = 0;
   std::thread loop;
 };
 
 namespace {
 
 constexpr size_t kCacheCap = size_t(8) << 30;  // pinned bytes kept for later jobs
+constexpr int kGroupMax = 16;                    // buffers started together at most
+// Buffers from this size on keep the combined copy-and-process call, which
+// overlaps the copy of each channel group with its processing; smaller ones
+// are copied whole anyway and may share launches with other jobs' buffers.
+constexpr size_t kGroupMaxBytes = size_t(16) << 20;
 
 char* take_pinned(rawspec_gb300_server* s, size_t bytes, size_t* cap) {
   {
@@ -226,6 +235,92 @@ void request_loop(rawspec_gb300_server* s) {
     }
 
     bool progress = false, busy = false;
+    // Jobs whose next buffer can start: with two or more, their buffers are
+    // copied and then started together, so that launches of the same kernel
+    // configuration share one grid (rawspec_gb300_start_processing_group).
+    if (s->group) {
+      std::vector<Job*> ready;
+      for (auto& kv : s->jobs) {
+        Job* j = kv.second.get();
+        if (j->state != RAWSPEC_GB300_JOB_ACTIVE || j->queue.empty() || (int)ready.size() >= kGroupMax) continue;
+        size_t in_bytes = 0;
+        rawspec_gb300_device_input(&j->ctx, &in_bytes);
+        if (in_bytes >= kGroupMaxBytes) continue;  // the pipelined single call serves it better
+        if (j->inflight) {
+          lk.unlock();
+          const bool idle = rawspec_check_for_completion(&j->ctx) != 0;
+          lk.lock();
+          if (!idle) continue;
+          j->inflight = false;
+          j->buffers++;
+          j->buf_lat.push_back(1e3 * (now_s() - j->cur.t_push));
+          progress = true;
+        }
+        ready.push_back(j);
+      }
+      // only jobs that share a small-FFT kernel configuration with another
+      // ready job gain from starting together; the others keep the single call
+      {
+        std::map<long long, int> count;
+        std::vector<std::vector<long long>> keys(ready.size());
+        for (size_t r = 0; r < ready.size(); r++) {
+          const rawspec_context& c = ready[r]->ctx;
+          for (unsigned i = 0; i < c.No; i++)
+            if (rawspec_gb300_product_kernel(const_cast<rawspec_context*>(&c), (int)i) == RAWSPEC_GB300_K_SMALL)
+              keys[r].push_back(((long long)c.Nts[i] << 16) | ((long long)c.Nbps << 8) | ((long long)c.Np << 4) |
+                                (long long)(c.Npolout[i] + 4));
+          std::sort(keys[r].begin(), keys[r].end());
+          keys[r].erase(std::unique(keys[r].begin(), keys[r].end()), keys[r].end());
+          for (long long k : keys[r]) count[k]++;
+        }
+        std::vector<Job*> shared;
+        for (size_t r = 0; r < ready.size(); r++) {
+          bool any = false;
+          for (long long k : keys[r]) any = any || count[k] >= 2;
+          if (any) shared.push_back(ready[r]);
+        }
+        ready.swap(shared);
+      }
+      if (ready.size() >= 2) {
+        for (Job* j : ready) {
+          j->cur = j->queue.front();
+          j->queue.pop_front();
+        }
+        lk.unlock();
+        std::vector<rawspec_context*> ctxs;
+        std::vector<int> dirs;
+        int rc = 0;
+        for (Job* j : ready) {
+          for (unsigned b = 0; b < j->ctx.Nb; b++) j->blocks[b] = j->cur.data + b * j->blk_bytes;
+          j->t_inflight.store(j->cur.t_push);
+          rc |= j->expand4 ? rawspec_copy_blocks_to_gpu_expanding_complex4(&j->ctx, 0, 0, j->ctx.Nb)
+                           : rawspec_copy_blocks_to_gpu(&j->ctx, 0, 0, j->ctx.Nb);
+          ctxs.push_back(&j->ctx);
+          dirs.push_back(j->fft_dir);
+        }
+        if (rc == 0) rc = rawspec_gb300_start_processing_group(ctxs.data(), dirs.data(), (int)ctxs.size());
+        if (rc == 0) s->group_calls++;
+        lk.lock();
+        for (Job* j : ready) {
+          j->free_slots.push_back(j->cur.data);  // the copies have completed
+          j->inflight = true;
+        }
+        s->cv_state.notify_all();
+        progress = true;
+        busy = true;
+        if (rc) {
+          for (Job* j : ready) {
+            lk.unlock();
+            rawspec_wait_for_completion(&j->ctx);
+            rawspec_cleanup(&j->ctx);
+            lk.lock();
+            j->inflight = false;
+            free_pool(s, j);
+            retire(s, j, RAWSPEC_GB300_JOB_FAILED);
+          }
+        }
+      }
+    }
     for (auto& kv : s->jobs) {
       Job* j = kv.second.get();
       if (j->state != RAWSPEC_GB300_JOB_ACTIVE) continue;
@@ -299,6 +394,7 @@ rawspec_gb300_server* rawspec_gb300_server_create(int gpu_index, size_t hbm_budg
   s->budget = hbm_budget;
   s->max_active = max_active;
   s->max_queued = max_queued;
+  if (const char* v = getenv("RAWSPEC_GB300_SERVE_GROUP")) s->group = v[0] != '0';
   try {
     s->loop = std::thread(request_loop, s);
   } catch (...) {
@@ -458,6 +554,7 @@ int rawspec_gb300_server_get_stats(rawspec_gb300_server* s, rawspec_gb300_server
   st->used = s->used;
   st->peak_used = s->peak_used;
   st->peak_active = s->peak_active;
+  st->group_calls = s->group_calls;
   st->buffer_p50_ms = pct(bl, 0.50);
   st->buffer_p99_ms = pct(bl, 0.99);
   st->dump_p50_ms = pct(dl, 0.50);

@@ -28,7 +28,7 @@ class ServerStats(C.Structure):
                 ("budget", C.c_size_t), ("used", C.c_size_t), ("peak_used", C.c_size_t), ("peak_active", C.c_int),
                 ("buffers", C.c_longlong), ("dumps", C.c_longlong),
                 ("buffer_p50_ms", C.c_double), ("buffer_p99_ms", C.c_double),
-                ("dump_p50_ms", C.c_double), ("dump_p99_ms", C.c_double)]
+                ("dump_p50_ms", C.c_double), ("dump_p99_ms", C.c_double), ("group_calls", C.c_longlong)]
 
 
 _declared = False
