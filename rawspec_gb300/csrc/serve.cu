@@ -114,6 +114,7 @@ struct rawspec_gb300_server {
   std::mutex mu;
   std::condition_variable cv_loop;   // work for the request loop
   std::condition_variable cv_state;  // job state changes and queue space
+  std::condition_variable cv_admit;  // pending jobs, or memory and slots freed
   std::map<int, std::unique_ptr<Job>> jobs;
   std::deque<int> pending;
   int next_id = 0;
@@ -124,6 +125,7 @@ struct rawspec_gb300_server {
   bool group = true;
   long long group_calls = 0;
   std::thread loop;
+  std::thread admitter;  // admission (pinned slots, context creation) off the request loop
 };
 
 namespace {
@@ -182,9 +184,14 @@ void retire(rawspec_gb300_server* s, Job* j, int state) {
   s->active--;
   s->used -= j->est;
   s->cv_state.notify_all();
+  s->cv_admit.notify_all();
 }
 
-void request_loop(rawspec_gb300_server* s) {
+// Admission in submission order, on a thread of its own: taking a job's
+// pinned slots and creating its context take milliseconds (tens for a large
+// job's first buffers of a size), during which the request loop keeps
+// feeding the active jobs.
+void admit_loop(rawspec_gb300_server* s) {
   cudaSetDevice(s->gpu);
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
@@ -232,8 +239,18 @@ void request_loop(rawspec_gb300_server* s) {
       j->state = RAWSPEC_GB300_JOB_ACTIVE;
       j->t_admit = now_s();
       s->cv_state.notify_all();
+      s->cv_loop.notify_all();
     }
 
+    if (s->stop && s->pending.empty()) break;
+    s->cv_admit.wait_for(lk, std::chrono::milliseconds(5));
+  }
+}
+
+void request_loop(rawspec_gb300_server* s) {
+  cudaSetDevice(s->gpu);
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
     bool progress = false, busy = false;
     // Jobs whose next buffer can start: with two or more, their buffers are
     // copied and then started together, so that launches of the same kernel
@@ -401,6 +418,18 @@ rawspec_gb300_server* rawspec_gb300_server_create(int gpu_index, size_t hbm_budg
     delete s;
     return nullptr;
   }
+  try {
+    s->admitter = std::thread(admit_loop, s);
+  } catch (...) {
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      s->stop = true;
+      s->cv_loop.notify_all();
+    }
+    s->loop.join();
+    delete s;
+    return nullptr;
+  }
   return s;
 }
 
@@ -452,7 +481,7 @@ int rawspec_gb300_server_submit(rawspec_gb300_server* s, const rawspec_context* 
   j->id = id;
   s->jobs[id] = std::move(j);
   s->pending.push_back(id);
-  s->cv_loop.notify_all();
+  s->cv_admit.notify_all();
   return id;
 }
 
@@ -569,7 +598,9 @@ void rawspec_gb300_server_destroy(rawspec_gb300_server* s) {
     for (auto& kv : s->jobs) kv.second->closed = true;
     s->stop = true;
     s->cv_loop.notify_all();
+    s->cv_admit.notify_all();
   }
+  s->admitter.join();  // admits the pending jobs (closed: they run their queued buffers and end)
   s->loop.join();
   for (auto& kv : s->jobs) free_pool(s, kv.second.get());
   for (auto& kv : s->cache) cudaFreeHost(kv.second);
