@@ -195,17 +195,19 @@ bool is_pow2(unsigned x) { return x && !(x & (x - 1)); }
 int ilog2u(unsigned x) { int l = 0; while ((1u << l) < x) ++l; return l; }
 
 // rawspec_start_processing replays CUDA graphs of its launches for input
-// buffers below 16 MiB, where the host's launch calls take as long as the
-// kernels; larger buffers launch directly (a graph of the production shape's
-// three products measured 2 % slower: its branches start in another order).
-// RAWSPEC_GB300_GRAPHS=1 / =0 (read at each call) selects graphs always /
-// never.
+// buffers below 128 MiB, where the host's launch calls are a measurable part
+// of a buffer's time (the 4-antenna 4-bit Stokes shape, 64 MiB expanded:
+// 0.243 against 0.250 ms per buffer); larger buffers launch directly (a graph
+// of the production shape's three products measured 1-2 % slower: its
+// branches start in another order).  RAWSPEC_GB300_GRAPHS=1 / =0 (read at
+// each call) selects graphs always / never.
 constexpr size_t kMaxGraphs = 64;
+constexpr size_t kMaxGraphedBytes = size_t(128) << 20;
 bool graphs_wanted(const GpuCtx* g) {
   const char* v = getenv("RAWSPEC_GB300_GRAPHS");
   if (v && v[0] == '0') return false;
   if (v && v[0] == '1') return true;
-  return g->in_bytes < kMinPipelinedBytes;
+  return g->in_bytes < kMaxGraphedBytes;
 }
 
 // Which products of 8-bit input run their DFT on the tensor cores (k_tc)
