@@ -121,6 +121,13 @@ struct FusedCfg {
   // store covers whole 128-byte lines (its 32 / C_A values of j span the
   // block); where a warp spans fewer than C_B values of j, BK = 1 (rows).
   static constexpr int BK = (CB <= 32 / CA) ? CB : 1;
+  // With BK = C_B the two polarisations are interleaved, [k2 / BK][n1][k2 %
+  // BK] of 16 bytes (re pol 0, re pol 1, im pol 0, im pol 1: the packed pair
+  // as the registers hold it): a column tile stores both values of a bin
+  // with one 16-byte store, a row tile's input is one contiguous block of
+  // both polarisations that lands in two halves of N1 / 2 values n1 (one per
+  // stage buffer), and a row thread reads both values with one 16-byte load.
+  static constexpr bool IL = BK == CB && (N1 / 2) % TB == 0;
   static constexpr unsigned BYTES_A = (unsigned)N2 * CW * 4;
   static constexpr unsigned BYTES_TW = (unsigned)(TA + RA) * CA * 8;
   static constexpr unsigned BYTES_B = (unsigned)CB * N1 * 8;
@@ -134,6 +141,13 @@ struct FusedCfg {
 template <int N1, int N2, int BK>
 __device__ __forceinline__ size_t ring_index(int q, int k2, int n1) {
   return ((size_t)q * N2 + (size_t)(k2 / BK) * BK) * N1 + (size_t)n1 * BK + (k2 % BK);
+}
+
+// Offset, in float4 (both polarisations of a value), of element (k2, n1) in
+// the interleaved layout of a ring slot.
+template <int N1, int BK>
+__device__ __forceinline__ size_t ring_index_il(int k2, int n1) {
+  return (size_t)(k2 / BK) * BK * N1 + (size_t)n1 * BK + (k2 % BK);
 }
 
 struct Sync {
@@ -202,6 +216,11 @@ __device__ __forceinline__ unsigned long long policy_evict_last() {
 }
 __device__ __forceinline__ void st_f2_hint(float2* p, float2 v, unsigned long long pol) {
   asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st_f4_hint(float4* p, float4 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+               "f"(v.w), "l"(pol)
                : "memory");
 }
 __device__ __forceinline__ void st_f_hint(float* p, float v, unsigned long long pol) {
@@ -403,9 +422,10 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
       tma_load_2d(tw + F::TA * F::CA, &a.tmap_twm, tile * F::CA, 0, mb, pol_last);
     } else {
       const int tile = it.titem * K + (s >> 1);
-      const int q = s & 1;
-      const float2* src =
-          a.scratch + (size_t)(it.slab % a.ring) * 2 * N + ((size_t)q * N2 + (size_t)tile * F::CB) * N1;
+      const int q = s & 1;  // interleaved: half q of the tile's block; else polarisation q
+      const float2* slotp = a.scratch + (size_t)(it.slab % a.ring) * 2 * N;
+      const float2* src = F::IL ? slotp + ((size_t)2 * tile + q) * F::CB * N1
+                                : slotp + ((size_t)q * N2 + (size_t)tile * F::CB) * N1;
       mbar_expect_tx(mb, F::BYTES_B);
       if constexpr (F::BK == F::CB) {
         bulk_load(dst, src, F::BYTES_B, mb);  // one block [n1][C_B rows]
@@ -500,8 +520,13 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
           // W_N^(n1 k2) = W_N^(n1 j) W_N^(n1 m T)
           const float2 twk = m == 0 ? w0 : cmul(w0, tw[(T + m) * C + col]);
           const cpair x = pmul(v[m], twk);
-          st_f2_hint(dst + ring_index<N1, N2, F::BK>(0, k2, n1), lane0(x), pol_last);
-          st_f2_hint(dst + ring_index<N1, N2, F::BK>(1, k2, n1), lane1(x), pol_last);
+          if constexpr (F::IL) {
+            st_f4_hint(reinterpret_cast<float4*>(dst) + ring_index_il<N1, F::BK>(k2, n1),
+                       make_float4(x.re.x, x.re.y, x.im.x, x.im.y), pol_last);
+          } else {
+            st_f2_hint(dst + ring_index<N1, N2, F::BK>(0, k2, n1), lane0(x), pol_last);
+            st_f2_hint(dst + ring_index<N1, N2, F::BK>(1, k2, n1), lane1(x), pol_last);
+          }
         }
       }
       publish(doneA + it.slab, K);
@@ -545,14 +570,38 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
           cpair vp[R];
           mbar_wait(&mbar[0], ph & 1u, err, &s_abort);
           ph ^= 1u;
+          if constexpr (F::IL) {
+            // values n1 < N1/2 in buffer 0, the others in buffer 1
+            constexpr int MH = N1 / 2 / T;
+            const float4* h0 = reinterpret_cast<const float4*>(sb0) + (size_t)j * C + row;
+            const float4* h1 = reinterpret_cast<const float4*>(sb1) + (size_t)j * C + row;
 #pragma unroll
-          for (int m = 0; m < R; ++m) v[0][m] = sb0[row_slot(j + m * T)];
-          mbar_wait(&mbar[1], (ph >> 1) & 1u, err, &s_abort);
-          ph ^= 2u;
+            for (int m = 0; m < MH; ++m) {
+              const float4 f = h0[(size_t)m * T * C];
+              vp[m] = cpair{make_float2(f.x, f.y), make_float2(f.z, f.w)};
+            }
+            mbar_wait(&mbar[1], (ph >> 1) & 1u, err, &s_abort);
+            ph ^= 2u;
 #pragma unroll
-          for (int m = 0; m < R; ++m) vp[m] = pack2(v[0][m], sb1[row_slot(j + m * T)]);
+            for (int m = MH; m < R; ++m) {
+              const float4 f = h1[(size_t)(m - MH) * T * C];
+              vp[m] = cpair{make_float2(f.x, f.y), make_float2(f.z, f.w)};
+            }
+          } else {
+#pragma unroll
+            for (int m = 0; m < R; ++m) v[0][m] = sb0[row_slot(j + m * T)];
+            mbar_wait(&mbar[1], (ph >> 1) & 1u, err, &s_abort);
+            ph ^= 2u;
+#pragma unroll
+            for (int m = 0; m < R; ++m) vp[m] = pack2(v[0][m], sb1[row_slot(j + m * T)]);
+          }
 #if RSG_FUSED_DISCARD
-          {
+          if constexpr (F::IL) {
+            const char* blk = reinterpret_cast<const char*>(scr + (size_t)2 * tile * C * N1);
+            constexpr int kLines = 2 * F::BYTES_B / 128;
+#pragma unroll 1
+            for (int l = tid; l < kLines; l += kFusedTPB) discard_l2(blk + (size_t)l * 128);
+          } else {
             const char* rows0 = reinterpret_cast<const char*>(scr + (size_t)tile * C * N1);
             const char* rows1 = reinterpret_cast<const char*>(scr + ((size_t)N2 + (size_t)tile * C) * N1);
             constexpr int kLines = F::BYTES_B / 128;
