@@ -114,6 +114,13 @@ cudaError_t tc_table_fill(void* dst, int logN, cudaStream_t s);
 // partial_floats receives the scratch the launches need.  0, or -1.
 int tc_configure(TcLaunch& L, size_t* partial_floats, int pipe_groups);
 cudaError_t tc_launch(const TcLaunch& L, cudaStream_t s);
+// The one-stage tensor-core kernel for N = 8, 16, 32 (k_tcs.cu), reached
+// through the functions above.
+bool tcs_supported(int logN, int fmt, int nv, int pol, int M);
+size_t tcs_table_bytes(int logN);
+cudaError_t tcs_table_fill(void* dst, int logN, cudaStream_t s);
+cudaError_t tcs_plan(const TcLaunch& L, int* occ, size_t* smem);  // resident CTAs per SM, padded shared memory
+cudaError_t tcs_launch(const TcLaunch& L, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Four-step large FFT (4096 < N <= 2^22): N = N1 * N2.

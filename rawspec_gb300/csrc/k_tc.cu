@@ -67,15 +67,6 @@ namespace {
 
 constexpr long long kTcWaitCycles = 2000000000ll;  // ~1 s of SM clocks for an MMA batch
 
-// Two int8 (re, im) codes of one word -> an FP16 pair, exactly: the bytes
-// (offset by 128) become the low mantissa bits of 1024 + v, then 1152 is
-// subtracted.  sel picks polarisation 0 (0x4140) or 1 (0x4342).
-__device__ __forceinline__ uint32_t codes_to_h2(uint32_t x, uint32_t sel) {
-  const uint32_t b = __byte_perm(x, 0x64646464u, sel);
-  uint32_t r;
-  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(b), "r"(0x64806480u));
-  return r;
-}
 
 }  // namespace
 
@@ -154,8 +145,8 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const uint32_t x = __vmaxs4(w[4 * g4 + i], 0x81818181u) ^ 0x80808080u;
-        h0[i] = codes_to_h2(x, 0x4140);
-        h1[i] = codes_to_h2(x, 0x4342);
+        h0[i] = tc::codes_to_h2(x, 0x4140);
+        h1[i] = tc::codes_to_h2(x, 0x4342);
       }
       const int kc = n1_0 / 4 + g4;
       const int m0 = (2 * lsp) * S + ln2, m1 = m0 + S;
@@ -490,6 +481,7 @@ int tc_spc(int M, int spt, int units, int slots) {
 }  // namespace
 
 bool tc_supported(int logN, int fmt, int nv, int pol, int M) {
+  if (logN <= 5) return tcs_supported(logN, fmt, nv, pol, M);
   if (fmt != FMT_I8 || nv != 2) return false;
   if (logN != 8 && logN != 10 && logN != 12) return false;
   if (logN == 12 && pol != POL_TP) return false;
@@ -497,6 +489,7 @@ bool tc_supported(int logN, int fmt, int nv, int pol, int M) {
 }
 
 size_t tc_table_bytes(int logN) {
+  if (logN <= 5) return tcs_table_bytes(logN);
   switch (logN) {
     case 8: return TcCfg<16>::TAB_BYTES;
     case 10: return TcCfg<32>::TAB_BYTES;
@@ -510,6 +503,7 @@ cudaError_t tc_table_fill(void* dst, int logN, cudaStream_t s) {
   if (!bytes) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(dst, 0, bytes, s);
   if (e != cudaSuccess) return e;
+  if (logN <= 5) return tcs_table_fill(dst, logN, s);
   unsigned char* t = static_cast<unsigned char*>(dst);
   switch (logN) {
     case 8: k_tc_tables<16><<<(TcCfg<16>::ND * TcCfg<16>::K + 255) / 256, 256, 0, s>>>(t); break;
@@ -521,15 +515,23 @@ cudaError_t tc_table_fill(void* dst, int logN, cudaStream_t s) {
 
 int tc_configure(TcLaunch& L, size_t* partial_floats, int pipe_groups) {
   if (L.M < 1 || L.n_units < 1) return -1;
-  int occ = 0, sms = 0, dev = 0;
+  int occ = 0, sms = 0, dev = 0, spt = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
-      cudaSuccess || tc_dispatch(L, nullptr, 2, &occ) != cudaSuccess || occ < 1)
+      cudaSuccess)
     return -1;
-  const int S = tc_side(L.logN), spt = 64 / S;
-  const int tmem_cols = 8 * S;
-  occ = std::min(occ, 512 / tmem_cols);  // tensor-memory columns of the SM
+  if (L.logN <= 5) {  // one-stage kernel k_tcs: 64 spectra per tile
+    size_t smem = 0;
+    if (tcs_plan(L, &occ, &smem) != cudaSuccess || occ < 1) return -1;
+    spt = 64;
+    L.smem = smem;
+  } else {
+    if (tc_dispatch(L, nullptr, 2, &occ) != cudaSuccess || occ < 1) return -1;
+    const int S = tc_side(L.logN);
+    spt = 64 / S;
+    occ = std::min(occ, 512 / (8 * S));  // tensor-memory columns of the SM
+    L.smem = (L.logN == 8) ? TcCfg<16>::SMEM : (L.logN == 10) ? TcCfg<32>::SMEM : TcCfg<64>::SMEM;
+  }
   L.slots = occ * sms;
-  L.smem = (L.logN == 8) ? TcCfg<16>::SMEM : (L.logN == 10) ? TcCfg<32>::SMEM : TcCfg<64>::SMEM;
   L.spc = tc_spc(L.M, spt, L.n_units, L.slots);
   L.chunks = (L.M + L.spc - 1) / L.spc;
   const int gunits = std::max(1, L.n_units / std::max(1, pipe_groups));
@@ -547,6 +549,8 @@ int tc_configure(TcLaunch& L, size_t* partial_floats, int pipe_groups) {
   return 0;
 }
 
-cudaError_t tc_launch(const TcLaunch& L, cudaStream_t s) { return tc_dispatch(L, s, 0); }
+cudaError_t tc_launch(const TcLaunch& L, cudaStream_t s) {
+  return L.logN <= 5 ? tcs_launch(L, s) : tc_dispatch(L, s, 0);
+}
 
 }  // namespace rsg

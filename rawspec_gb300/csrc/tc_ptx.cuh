@@ -79,6 +79,17 @@ __device__ __forceinline__ void mma_commit(uint64_t* mbar) {
                : "memory");
 }
 
+// ---- operands ----
+// Two int8 (re, im) codes of one word -> an FP16 pair, exactly: the bytes
+// (offset by 128) become the low mantissa bits of 1024 + v, then 1152 is
+// subtracted.  sel picks polarisation 0 (0x4140) or 1 (0x4342).
+__device__ __forceinline__ uint32_t codes_to_h2(uint32_t x, uint32_t sel) {
+  const uint32_t b = __byte_perm(x, 0x64646464u, sel);
+  uint32_t r;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(b), "r"(0x64806480u));
+  return r;
+}
+
 // ---- mbarrier ----
 __device__ __forceinline__ void mbar_init(uint64_t* mb, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb)), "r"(count) : "memory");
@@ -106,6 +117,26 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mb, unsigned parity,
 }
 
 // ---- tensor memory -> registers ----
+// One load of 16 consecutive columns of this thread's lane (32x32b shape),
+// then the wait; the registers are tied to the wait so that no use of them
+// can be scheduled before it.
+__device__ __forceinline__ void tmem_ld16(uint32_t ta, float (&a)[16]) {
+  uint32_t* ra = reinterpret_cast<uint32_t*>(a);
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(ra[0]), "=r"(ra[1]), "=r"(ra[2]), "=r"(ra[3]), "=r"(ra[4]), "=r"(ra[5]), "=r"(ra[6]), "=r"(ra[7]),
+        "=r"(ra[8]), "=r"(ra[9]), "=r"(ra[10]), "=r"(ra[11]), "=r"(ra[12]), "=r"(ra[13]), "=r"(ra[14]),
+        "=r"(ra[15])
+      : "r"(ta));
+  asm volatile(
+      "tcgen05.wait::ld.sync.aligned;"
+      : "+r"(ra[0]), "+r"(ra[1]), "+r"(ra[2]), "+r"(ra[3]), "+r"(ra[4]), "+r"(ra[5]), "+r"(ra[6]), "+r"(ra[7]),
+        "+r"(ra[8]), "+r"(ra[9]), "+r"(ra[10]), "+r"(ra[11]), "+r"(ra[12]), "+r"(ra[13]), "+r"(ra[14]),
+        "+r"(ra[15])
+      :
+      : "memory");
+}
 // Two loads of 16 consecutive columns of this thread's lane (32x32b shape),
 // then the wait; the registers are tied to the wait so that no use of them
 // can be scheduled before it.

@@ -4,9 +4,10 @@ FP32 accumulation in tensor memory) against the FP64 oracle.
 First the MMA building block alone: a host-built shared-memory image of two
 K-major FP16 operands goes through the library's descriptors and MMA
 wrappers (tests/probe/umma_probe.cu) and must give the exact integer matrix
-product.  Then whole products with RAWSPEC_GB300_TENSOR_DFT=1 (the kernel
-for every length it supports: 256, 1024, 4096), every mode, direction,
-integration spanning buffers and the pipelined combined call.  The errors
+product.  Then whole products with RAWSPEC_GB300_TENSOR_DFT=1 (the kernels
+for every length they support: the one-stage k_tcs at 8, 16, 32, the
+two-stage k_tc at 256, 1024, 4096), every mode, direction, integration
+spanning buffers and the pipelined combined call.  The errors
 against the oracle are printed (pytest -s) as well as checked."""
 import ctypes as C
 import subprocess
@@ -98,6 +99,8 @@ def oracle_for(c, blocks):
 
 
 @pytest.mark.parametrize("logn,npol,na,conj,fft_dir", [
+    (3, 1, 128, 0, 1), (3, 4, 64, 1, 1), (3, -4, 256, 1, -1), (4, 1, 64, 0, -1), (4, -4, 128, 1, 1),
+    (5, 1, 64, 0, 1), (5, 4, 128, 1, -1), (5, -4, 64, 0, 1),
     (8, 1, 16, 0, 1), (8, 4, 8, 1, 1), (8, -4, 64, 1, -1),
     (10, 1, 8, 0, 1), (10, 4, 2, 1, -1), (10, -4, 16, 0, 1), (10, 1, 32, 1, -1),
     (12, 1, 4, 0, 1), (12, 1, 1, 0, -1)])
@@ -114,20 +117,21 @@ def test_tensor_dft_matches_oracle(cuda_device, monkeypatch, logn, npol, na, con
     assert err < REL_TOL, (nt, npol, err)
 
 
-@pytest.mark.parametrize("npol", [1, 4])
-def test_tensor_dft_integration_across_buffers(cuda_device, monkeypatch, npol):
-    # 16 spectra per channel per buffer, integrations of 96 spectra: six
-    # buffers per dump (the accumulation into the dump buffer) and units
-    # spread over several CTAs (partial sums + k_finalize)
-    nt, Ntpb = 1024, 1 << 14
-    c = dict(Nc=2, Np=2, Ntpb=Ntpb, nbits=8, nblocks=6, products=[(nt, 96, npol)], conj=1, fft_dir=1)
+@pytest.mark.parametrize("nt,npol", [(1024, 1), (1024, 4), (8, 1), (16, -4)])
+def test_tensor_dft_integration_across_buffers(cuda_device, monkeypatch, nt, npol):
+    # one block of spectra per channel per buffer, integrations of six
+    # buffers (the accumulation into the dump buffer), units spread over
+    # several CTAs (partial sums + k_finalize)
+    Ntpb = 1 << 14
+    na = 6 * Ntpb // nt
+    c = dict(Nc=2, Np=2, Ntpb=Ntpb, nbits=8, nblocks=6, products=[(nt, na, npol)], conj=1, fft_dir=1)
     blocks = synth.gaussian_blocks(6, 2, Ntpb, 2, sigma=20.0, seed=811 + npol)
     got, n_tc, _ = run_tc(monkeypatch, c, blocks)
     assert n_tc > 0
     ref = oracle_for(c, blocks)
     assert got[0].shape == ref[0].shape
     err = normalized_error(got[0], ref[0], npol, 2, nt)
-    print(f"k_tc N={nt} Npolout={npol} Na=96 over six buffers: normalized error {err:.2e}")
+    print(f"k_tc N={nt} Npolout={npol} Na={na} over six buffers: normalized error {err:.2e}")
     assert err < REL_TOL
 
 
