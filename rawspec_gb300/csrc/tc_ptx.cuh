@@ -106,6 +106,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mb, unsigned parity) {
       : "memory");
   return ok != 0;
 }
+// One plain arrival (release semantics at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t* mb) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mb)) : "memory");
+}
+// One arrival that also expects `bytes` of asynchronous copies on the barrier.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mb, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mb)), "r"(bytes) : "memory");
+}
+// Bulk copy global -> shared (16-byte aligned addresses, size a multiple of
+// 16), completing `bytes` transactions on the barrier.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* mb) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(mb))
+               : "memory");
+}
 // Waits for the phase of the given parity, at most `limit` SM clock cycles;
 // false on time-out.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mb, unsigned parity, long long limit) {
