@@ -173,3 +173,18 @@ def test_cpu_fp32_chain_matches_oracle(name):
     outs, icss = O.run_cpu(cfg, g["blocks"], nthreads=2)
     for i, (nt, na, npol) in enumerate(c["products"]):
         assert normalized_error(outs[i], g[f"out{i}"], npol, c["Nc"], nt) < 1e-4
+
+
+@pytest.mark.parametrize("logn,npol,inverse", [(15, 1, 0), (17, 4, 1), (16, -4, 0), (3, 4, 1), (9, 1, 0)])
+def test_cpu_fp32_chain_long_and_short_transforms(logn, npol, inverse):
+    # the CPU chain's FFT: Stockham radix-4 up to 16384 points, the four-step
+    # split above, against the FP64 oracle on the same seeded input
+    from util import normalized_error
+    from rawspec_gb300 import synth
+    nt = 1 << logn
+    ntpb = max(nt, 1 << 14)
+    blocks = synth.gaussian_blocks(1, 2, ntpb, 2, sigma=20.0, seed=logn)
+    cfg = O.make_cfg(2, 2, ntpb, 1, 8, [(nt, 1, npol)], inverse=inverse)
+    ref = O.run_oracle(cfg, blocks)[0][0]
+    got = O.run_cpu(cfg, blocks, nthreads=2)[0][0]
+    assert normalized_error(got, ref, npol, 2, nt) < 1e-5
