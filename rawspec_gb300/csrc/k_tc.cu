@@ -204,11 +204,16 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int k1 = 8 * q + i;
-        const float2 y = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
-        const float2 tv = cmul(y, twv[i]);
+        // (re, im) pairs on the packed instructions: y = hi + lo products,
+        // y w, and the residual below the FP16 part
+        const float2 y = __fadd2_rn(make_float2(h[2 * i], h[2 * i + 1]), make_float2(l[2 * i], l[2 * i + 1]));
+        const float2 w = twv[i];
+        const float2 tv = __ffma2_rn(make_float2(-y.y, y.y), make_float2(w.y, w.x),
+                                     __fmul2_rn(make_float2(y.x, y.x), w));
         const __half2 hi = __floats2half2_rn(tv.x, tv.y);
         const float2 hf = __half22float2(hi);
-        const __half2 lo = __floats2half2_rn(tv.x - hf.x, tv.y - hf.y);
+        const float2 res = __ffma2_rn(hf, make_float2(-1.0f, -1.0f), tv);
+        const __half2 lo = __floats2half2_rn(res.x, res.y);
         const int mr = seq * S + k1;
         const int off = (mr >> 3) * C::SBO + (r >> 2) * C::LBO + (mr & 7) * 16 + (r & 3) * 4;
         *reinterpret_cast<__half2*>(sAhi + off) = hi;
@@ -217,7 +222,8 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
     }
   };
   // detection: lane seq S + k1 holds X[k1 + S k2] for all k2
-  auto epi2 = [&](float (&acc)[NACC]) {
+  constexpr int NACC2 = POL == POL_TP ? S / 2 : 1;  // total power: packed (x^2, y^2) sums
+  auto epi2 = [&](float (&acc)[NACC], float2 (&acc2)[NACC2]) {
 #pragma unroll
     for (int qq = 0; qq < NQ; ++qq) {
       const int q = 2 * qq + half;
@@ -225,15 +231,11 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
       tc::tmem_ld16x2(d2 + lane_off + 16 * q, d2 + lane_off + 2 * S + 16 * q, h, l);
       float2 X[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) X[i] = make_float2(h[2 * i] + l[2 * i], h[2 * i + 1] + l[2 * i + 1]);
+      for (int i = 0; i < 8; ++i) X[i] = __fadd2_rn(make_float2(h[2 * i], h[2 * i + 1]), make_float2(l[2 * i], l[2 * i + 1]));
       if constexpr (POL == POL_TP) {
+        // (sum x^2, sum y^2) per bin on the packed instructions
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          float s = acc[8 * qq + i];
-          s = __fmaf_rn(X[i].x, X[i].x, s);
-          s = __fmaf_rn(X[i].y, X[i].y, s);
-          acc[8 * qq + i] = s;
-        }
+        for (int i = 0; i < 8; ++i) acc2[8 * qq + i] = __ffma2_rn(X[i], X[i], acc2[8 * qq + i]);
       } else {
         // the other polarisation of the same spectrum and k1 is lane tid ^ S
         float2 Y[8];
@@ -288,6 +290,9 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
     float acc[NACC];
 #pragma unroll
     for (int i = 0; i < NACC; ++i) acc[i] = 0.0f;
+    float2 acc2[NACC2];
+#pragma unroll
+    for (int i = 0; i < NACC2; ++i) acc2[i] = make_float2(0.0f, 0.0f);
 
     // prologue: tile 0 through stage 1 and into stage 2
     load(src);
@@ -310,7 +315,7 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
         if (tid == 0) issue_s1();
       }
       wait(mb2, ph2);
-      epi2(acc);
+      epi2(acc, acc2);
       if (more) {
         wait(mb1, ph1);
         epi1();
@@ -325,7 +330,8 @@ __global__ void __launch_bounds__(TcCfg<S>::THREADS, TcCfg<S>::MINB) k_tc(const 
     // bin k1 + S k2 of this thread: k2 = 8 (2 qq + half) + i for its acc[8 qq + i]
     if constexpr (POL == POL_TP) {
 #pragma unroll
-      for (int j = 0; j < S / 2; ++j) red[seq * N + r + S * (8 * (2 * (j / 8) + half) + j % 8)] = acc[j];
+      for (int j = 0; j < S / 2; ++j)
+        red[seq * N + r + S * (8 * (2 * (j / 8) + half) + j % 8)] = acc2[j].x + acc2[j].y;
     } else {
       const int sp = seq >> 1, pl = seq & 1;
 #pragma unroll
