@@ -118,9 +118,14 @@ __device__ __forceinline__ void small_body(const SmallLaunch& a, const int bid) 
   // Total power of two polarisations on the packed instructions: one lane
   // per polarisation, the lanes summed after the last spectrum.
   constexpr bool kPackedTP = POL == POL_TP && NV == 2 && RSG_PACKED;
-  float2 acc2[kPackedTP ? R : 1];
+  // Cross products of two polarisations: the two powers as one packed pair
+  // (|X0|^2, |X1|^2), the cross terms Re and Im(X0 X1*) unsigned; Stokes I
+  // and Q and the conjugation sign are linear in these sums and applied
+  // after the last spectrum.
+  constexpr bool kPackedX = POL != POL_TP && NV == 2 && RSG_PACKED;
+  float2 acc2[(kPackedTP || kPackedX) ? R : 1];
 #pragma unroll
-  for (int m = 0; m < (kPackedTP ? R : 1); ++m) acc2[m] = make_float2(0.f, 0.f);
+  for (int m = 0; m < ((kPackedTP || kPackedX) ? R : 1); ++m) acc2[m] = make_float2(0.f, 0.f);
 
   float2* my_xch = xch + (size_t)g * NV * smem_padded_len(N);
 
@@ -203,6 +208,15 @@ __device__ __forceinline__ void small_body(const SmallLaunch& a, const int bid) 
           const cpair x = pack2(v[0][m], v[1][m]);
           acc2[m] = f2fma(x.im, x.im, f2fma(x.re, x.re, acc2[m]));
         }
+      } else if constexpr (kPackedX) {
+#pragma unroll
+        for (int m = 0; m < R; ++m) {
+          const float2 x0 = v[0][m], x1 = v[1][m];
+          const cpair x = pack2(x0, x1);
+          acc2[m] = f2fma(x.im, x.im, f2fma(x.re, x.re, acc2[m]));
+          acc[m][2] = __fmaf_rn(x0.y, x1.y, __fmaf_rn(x0.x, x1.x, acc[m][2]));
+          acc[m][3] = __fmaf_rn(-x0.x, x1.y, __fmaf_rn(x0.y, x1.x, acc[m][3]));
+        }
       } else {
 #pragma unroll
         for (int m = 0; m < R; ++m) {
@@ -217,6 +231,19 @@ __device__ __forceinline__ void small_body(const SmallLaunch& a, const int bid) 
   if constexpr (kPackedTP) {
 #pragma unroll
     for (int m = 0; m < R; ++m) acc[m][0] = acc2[m].x + acc2[m].y;
+  }
+  if constexpr (kPackedX) {
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      if constexpr (POL == POL_FULL) {
+        acc[m][0] = acc2[m].x;
+        acc[m][1] = acc2[m].y;
+      } else {
+        acc[m][0] = acc2[m].x + acc2[m].y;
+        acc[m][1] = acc2[m].x - acc2[m].y;
+      }
+      acc[m][3] *= im_sign;
+    }
   }
 
   // Reduce across the groups of each set: red[g][p][m][j], the groups'
