@@ -625,10 +625,13 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
               tp[m] = pw.x + pw.y;
             }
           } else {
+            // cross products: x0 = (|X0|^2, |X1|^2) from the packed pair,
+            // v[0] = (Re, Im)(X0 X1*)
 #pragma unroll
             for (int m = 0; m < R; ++m) {
-              x0[m] = lane0(vp[m]);
-              v[0][m] = lane1(vp[m]);
+              const float2 a0 = lane0(vp[m]), a1 = lane1(vp[m]);
+              x0[m] = f2fma(vp[m].im, vp[m].im, f2mul(vp[m].re, vp[m].re));
+              v[0][m] = make_float2(__fmaf_rn(a0.y, a1.y, a0.x * a1.x), __fmaf_rn(-a0.x, a1.y, a0.y * a1.x));
             }
           }
         }
@@ -664,10 +667,10 @@ k_large_fused(const __grid_constant__ LargeLaunch a) {
           if constexpr (POL == POL_TP) {
             acc[0] = tp[m];
           } else {
-#pragma unroll
-            for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
-            const float2 x[2] = {x0[m], v[0][m]};
-            detect_acc<POL, 2>(acc, x, im_sign);
+            acc[0] = POL == POL_FULL ? x0[m].x : x0[m].x + x0[m].y;
+            acc[1] = POL == POL_FULL ? x0[m].y : x0[m].x - x0[m].y;
+            acc[2] = v[0][m].x;
+            acc[3] = im_sign * v[0][m].y;
           }
           const int pos = out_pos(k2 + N2 * (j + m * T), N, a.inverse);
 #pragma unroll
