@@ -47,7 +47,7 @@ sys.path.insert(0, str(ROOT))
 NC, NP, NTPB, NBITS = 64, 2, 524288, 8
 PRODUCTS = [(1 << 20, 51), (8, 128), (1024, 3072)]
 SIGMA = 20.0
-E2E_REPS = 5
+E2E_REPS = 7  # end-to-end runs; the median stands against two runs slowed by host jitter
 BLOCK_BYTES = NC * NTPB * NP * 2
 WORKLOAD = "production shape: 64 ch x 2 pol int8, Ntpb 524288 (128 MiB blocks), Nfft 2^20/8/1024, Nint 51/128/3072"
 # The same config object on both arms (native and reference).
@@ -638,7 +638,7 @@ def run_native(args, rank, world, local_rank):
             wall.append(1e3 * (time.perf_counter() - ts))
         # end-to-end through the C-ABI from pinned host blocks: K steps of the
         # reference CLI's per-buffer sequence (rawspec.c:1012-1014), timed
-        # five times (host jitter moves single runs); the median is reported,
+        # E2E_REPS times (host jitter moves single runs); the median is reported,
         # every sample is kept
         nbuf = args.warmup + 3 * args.steps  # buffers processed so far
         for _ in range(args.warmup):
